@@ -1,0 +1,162 @@
+/* marbles_gb300.h -- C ABI of the GB300-native MARBLES level step.
+ *
+ * One opaque context owns every device buffer of one simulation (all AMR
+ * levels).  Calls on a context are serialised on its CUDA stream; a context is
+ * not re-entrant.  No call aborts or throws: each returns an mbg_status and
+ * mbg_last_error() gives the message of the last failure.
+ *
+ * Host arrays of per-cell data use the layout of an AMReX FArrayBox without
+ * ghost cells, concatenated over the boxes of the level in the order they
+ * were defined:   [box][component][k][j][i]   (i fastest).
+ *
+ * Reference interfaces (paths inside the NREL/marbles project) that these
+ * entry points replace are cited on each declaration.
+ */
+#ifndef MARBLES_GB300_H
+#define MARBLES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mbg_ctx mbg_ctx;
+
+typedef enum {
+    MBG_OK = 0,
+    MBG_EINVAL = 1,      /* bad argument or unsupported configuration        */
+    MBG_ENOMEM = 2,      /* device allocation failed                         */
+    MBG_ECUDA = 3,       /* a CUDA call failed                               */
+    MBG_ETIMEOUT = 4,    /* a bounded device-side wait ran out               */
+    MBG_ESTATE = 5       /* call out of order (e.g. level not defined)       */
+} mbg_status;
+
+/* storage / arithmetic forms of the populations */
+typedef enum {
+    MBG_FP64 = 0,          /* FP64 storage and arithmetic (the reference's)   */
+    MBG_FP32C_F16S = 1,    /* FP16 shifted storage, FP32 arithmetic           */
+    MBG_FP32C_BF16S = 2    /* BF16 shifted storage, FP32 arithmetic           */
+} mbg_precision;
+
+/* boundary-condition codes of lbm.bc_lo / lbm.bc_hi (Source/BC.H:13-20) */
+enum {
+    MBG_BC_PERIODIC = 0, MBG_BC_NOSLIP = 1, MBG_BC_VELOCITY = 2,
+    MBG_BC_PRESSURE = 3, MBG_BC_OUTFLOW = 5, MBG_BC_SLIPX = 6,
+    MBG_BC_SLIPY = 7, MBG_BC_SLIPZ = 8
+};
+
+/* lbm.velocity_bc_type (Source/VelocityBC.H:13-199) */
+enum { MBG_VBC_NOOP = 0, MBG_VBC_CONSTANT = 1, MBG_VBC_CHANNEL = 2, MBG_VBC_PARABOLIC = 3 };
+
+/* Per-simulation parameters.  Each field is the inputs key named beside it
+ * (Source/LBM.cpp:196-300, Source/VelocityBC.cpp:4-57). */
+typedef struct mbg_params {
+    int n_cell[3];               /* amr.n_cell (level 0)                       */
+    double prob_lo[3];           /* geometry.prob_lo                           */
+    double prob_hi[3];           /* geometry.prob_hi                           */
+    int is_periodic[3];          /* geometry.is_periodic                       */
+    int bc_lo[3], bc_hi[3];      /* lbm.bc_lo, lbm.bc_hi                        */
+    double nu;                   /* lbm.nu                                     */
+    double alpha;                /* lbm.alpha (defaults to nu)                 */
+    double dx_outer, dt_outer;   /* lbm.dx_outer, lbm.dt_outer                 */
+    double adiabatic_exponent;   /* lbm.adiabatic_exponent                     */
+    double m_bar;                /* lbm.mean_molecular_mass                    */
+    int precision;               /* mbg_precision                              */
+    /* reference state of the shifted 16-bit storage (ignored for FP64):
+     * populations are stored as (f - f_rest) / scale, f_rest the equilibrium
+     * at (rho_ref, u = 0, T_ref) */
+    double rho_ref, t_ref;
+    /* velocity BC functor (lbm.velocity_bc_type, velocity_bc_<type>.*) */
+    int velbc_type;
+    int vbc_dir;                 /* velocity_bc_constant.dir                   */
+    int vbc_normal_dir;          /* velocity_bc_parabolic.normal_dir           */
+    int vbc_tangential_dir;      /* velocity_bc_parabolic.tangential_dir       */
+    double vbc_u_ref;            /* Mach_ref * speed_of_sound_ref              */
+    double vbc_initial_density;
+    double vbc_initial_temperature;
+    double vbc_adiabatic_exponent;
+    double vbc_m_bar;
+} mbg_params;
+
+/* Create a context on the current CUDA device.  cuda_stream may be NULL (the
+ * context then creates its own stream).  Replaces the construction of the
+ * LBM object's level data (Source/LBM.cpp:6-151, LBM.H:25-319). */
+mbg_status mbg_create(const mbg_params* params, void* cuda_stream, mbg_ctx** out);
+
+/* Release every device buffer of the context. */
+void mbg_destroy(mbg_ctx* ctx);
+
+/* Message of the last failed call on this context (or of the last failed
+ * mbg_create when ctx is NULL). */
+const char* mbg_last_error(const mbg_ctx* ctx);
+
+/* Define level lev (0 = coarsest; ratio 2 between levels) from nbox boxes,
+ * lohi[6*n .. 6*n+5] = lo_x lo_y lo_z hi_x hi_y hi_z (inclusive, in the
+ * level's index space), and the is_fluid flags of each box grown by 3 ghost
+ * cells: flags[off_n + ((k+3)*(ny+6) + (j+3))*(nx+6) + (i+3)], bit 0 =
+ * is_fluid component 0, bit 1 = component 1 (eb_boundary), where off_n is the
+ * running sum of (nx+6)(ny+6)(nz+6) over the preceding boxes.  flags may be
+ * NULL (all fluid).  Levels must be defined in increasing order.
+ * Replaces MakeNewLevelFromScratch's MultiFab definitions and
+ * initialize_is_fluid (Source/LBM.cpp:1143-1262). */
+mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi,
+                            const uint8_t* flags);
+
+/* Number of valid cells of a level. */
+mbg_status mbg_level_cells(const mbg_ctx* ctx, int lev, long long* ncells);
+
+/* Upload / download f and g of a level (valid cells, FP64, 27 components).
+ * Replaces Initializer::initialize (Source/IC.H:460-525) on the way in and
+ * the MultiFab reads of plot/checkpoint output (Source/LBM.cpp:1629-1690)
+ * on the way out.  f or g may be NULL to skip it. */
+mbg_status mbg_set_state(mbg_ctx* ctx, int lev, const double* f, const double* g);
+mbg_status mbg_get_state(mbg_ctx* ctx, int lev, double* f, double* g);
+
+/* Macro fields of the current f, g (19 components in the order of
+ * Source/Constants.H:8-31: rho, vel_x, vel_y, vel_z, vel_mag, two_rho_e,
+ * QCorrX..Z, pxx, pyy, pzz, pxy, pxz, pyz, qx, qy, qz, temperature).
+ * Replaces LBM::f_to_macrodata (Source/LBM.cpp:810-906). */
+mbg_status mbg_get_macro(mbg_ctx* ctx, int lev, double* macro);
+
+/* One coarse time step of the whole hierarchy: ghost fill of level 0, then
+ * the recursive subcycled time_step (fine levels get 2 substeps per coarser
+ * step, explosion before them, coalescence after them).  Replaces
+ * LBM::evolve's loop body (Source/LBM.cpp:416-428) with time_step and
+ * advance (Source/LBM.cpp:452-544) and FillPatchOps::fillpatch / physbc
+ * (Source/FillPatchOps.H:75-159). */
+mbg_status mbg_step(mbg_ctx* ctx, int nsteps);
+
+/* One advance of a single level (stream + collide), without ghost fill
+ * and without coalescence.  Replaces LBM::advance for a level without a
+ * finer level (Source/LBM.cpp:523-544). */
+mbg_status mbg_advance_level(mbg_ctx* ctx, int lev);
+
+/* Fill the ghost cells of fine level lev > 0 from level lev-1 (explosion).
+ * Replaces FillPatchOps::fillpatch for lev > 0 (Source/FillPatchOps.H:
+ * 118-129, AMReX FillPatchTwoLevels with cell_cons_interp). */
+mbg_status mbg_fillpatch(mbg_ctx* ctx, int lev);
+
+/* Average fine level crse_lev+1 down onto level crse_lev over the covered
+ * cells grown by crse_ng (0 or 1) (coalescence).  Replaces
+ * LBM::average_down_to (Source/LBM.cpp:1571-1584) and
+ * average_down_with_ghosts (Source/Utilities.cpp:5-28). */
+mbg_status mbg_average_down(mbg_ctx* ctx, int crse_lev, int crse_ng);
+
+/* Momentum-exchange force on embedded-boundary cells summed over all levels
+ * (cells not covered by a finer level), FP64 accumulation.  Replaces
+ * LBM::compute_eb_forces (Source/LBM.cpp:994-1044). */
+mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3]);
+
+/* Wait for all work queued on the context's stream; reports a latched
+ * device-side error. */
+mbg_status mbg_synchronize(mbg_ctx* ctx);
+
+/* Number of kernel launches issued by the context since creation. */
+long long mbg_launch_count(const mbg_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MARBLES_GB300_H */

@@ -1,0 +1,198 @@
+"""GB300-native MARBLES level step: Python binding of libmarbles_gpu.so.
+
+The compute path is the CUDA library built from marbles_gb300/csrc; this
+module only marshals arguments through ctypes.  There is no CPU fallback:
+if the library is missing or cannot be loaded, every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmarbles_gpu.so")
+
+NQ = 27
+NMACRO = 19
+
+FP64, FP32C_F16S, FP32C_BF16S = 0, 1, 2
+STATUS = {0: "MBG_OK", 1: "MBG_EINVAL", 2: "MBG_ENOMEM", 3: "MBG_ECUDA", 4: "MBG_ETIMEOUT", 5: "MBG_ESTATE"}
+
+# every entry point declared in include/marbles_gb300.h
+EXPORTS = [
+    "mbg_create", "mbg_destroy", "mbg_last_error", "mbg_define_level", "mbg_level_cells",
+    "mbg_set_state", "mbg_get_state", "mbg_get_macro", "mbg_step", "mbg_advance_level",
+    "mbg_fillpatch", "mbg_average_down", "mbg_eb_forces", "mbg_synchronize", "mbg_launch_count",
+]
+
+
+class MbgError(RuntimeError):
+    pass
+
+
+class MbgParams(C.Structure):
+    """Mirror of struct mbg_params (include/marbles_gb300.h)."""
+    _fields_ = [
+        ("n_cell", C.c_int * 3),
+        ("prob_lo", C.c_double * 3), ("prob_hi", C.c_double * 3),
+        ("is_periodic", C.c_int * 3),
+        ("bc_lo", C.c_int * 3), ("bc_hi", C.c_int * 3),
+        ("nu", C.c_double), ("alpha", C.c_double),
+        ("dx_outer", C.c_double), ("dt_outer", C.c_double),
+        ("adiabatic_exponent", C.c_double), ("m_bar", C.c_double),
+        ("precision", C.c_int),
+        ("rho_ref", C.c_double), ("t_ref", C.c_double),
+        ("velbc_type", C.c_int),
+        ("vbc_dir", C.c_int), ("vbc_normal_dir", C.c_int), ("vbc_tangential_dir", C.c_int),
+        ("vbc_u_ref", C.c_double), ("vbc_initial_density", C.c_double),
+        ("vbc_initial_temperature", C.c_double), ("vbc_adiabatic_exponent", C.c_double),
+        ("vbc_m_bar", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    """Load the CUDA library (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise MbgError("libmarbles_gpu.so is not built (run __graft_entry__.build())")
+        L = C.CDLL(LIB_PATH)
+        vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+        L.mbg_create.argtypes = [C.POINTER(MbgParams), vp, C.POINTER(vp)]
+        L.mbg_destroy.argtypes = [vp]
+        L.mbg_destroy.restype = None
+        L.mbg_last_error.argtypes = [vp]
+        L.mbg_last_error.restype = C.c_char_p
+        L.mbg_define_level.argtypes = [vp, C.c_int, C.c_int, ip, C.POINTER(C.c_uint8)]
+        L.mbg_level_cells.argtypes = [vp, C.c_int, C.POINTER(C.c_longlong)]
+        L.mbg_set_state.argtypes = [vp, C.c_int, dp, dp]
+        L.mbg_get_state.argtypes = [vp, C.c_int, dp, dp]
+        L.mbg_get_macro.argtypes = [vp, C.c_int, dp]
+        L.mbg_step.argtypes = [vp, C.c_int]
+        L.mbg_advance_level.argtypes = [vp, C.c_int]
+        L.mbg_fillpatch.argtypes = [vp, C.c_int]
+        L.mbg_average_down.argtypes = [vp, C.c_int, C.c_int]
+        L.mbg_eb_forces.argtypes = [vp, dp]
+        L.mbg_synchronize.argtypes = [vp]
+        L.mbg_launch_count.argtypes = [vp]
+        L.mbg_launch_count.restype = C.c_longlong
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def default_params():
+    p = MbgParams()
+    p.n_cell[:] = [8, 8, 8]
+    p.prob_lo[:] = [0.0, 0.0, 0.0]
+    p.prob_hi[:] = [8.0, 8.0, 8.0]
+    p.is_periodic[:] = [1, 1, 1]
+    p.nu = 1.0
+    p.alpha = 1.0
+    p.dx_outer = 1.0
+    p.dt_outer = 1.0
+    p.adiabatic_exponent = 5.0 / 3.0
+    p.m_bar = 28.96
+    p.precision = FP64
+    p.rho_ref = 1.0
+    p.t_ref = 1.0 / 3.0
+    p.velbc_type = 0
+    p.vbc_dir = 1
+    p.vbc_normal_dir = 0
+    p.vbc_tangential_dir = 1
+    p.vbc_initial_density = 1.0
+    p.vbc_initial_temperature = 1.0 / 3.0
+    p.vbc_adiabatic_exponent = 5.0 / 3.0
+    p.vbc_m_bar = 28.96
+    return p
+
+
+class Context:
+    """One simulation on the GPU (all levels), through the C ABI."""
+
+    def __init__(self, params, stream=None):
+        self.L = lib()
+        self.p = params
+        h = C.c_void_p()
+        st = self.L.mbg_create(C.byref(params), stream, C.byref(h))
+        if st != 0:
+            raise MbgError("mbg_create: %s: %s" % (STATUS.get(st, st), self.L.mbg_last_error(None).decode()))
+        self.h = h
+        self.boxes = []
+
+    def _check(self, st, what):
+        if st != 0:
+            raise MbgError("%s: %s: %s" % (what, STATUS.get(st, st), self.L.mbg_last_error(self.h).decode()))
+
+    def define_level(self, lev, boxes, flags=None):
+        """boxes: (nbox, 6) lo/hi; flags: uint8 per grown-box cell or None."""
+        b = np.ascontiguousarray(boxes, dtype=np.int32)
+        fl = None
+        if flags is not None:
+            flags = np.ascontiguousarray(flags, dtype=np.uint8)
+            fl = flags.ctypes.data_as(C.POINTER(C.c_uint8))
+        self._check(self.L.mbg_define_level(self.h, lev, b.shape[0], b.ctypes.data_as(C.POINTER(C.c_int)), fl),
+                    "mbg_define_level")
+        self.boxes.append(b)
+
+    def ncells(self, lev):
+        n = C.c_longlong()
+        self._check(self.L.mbg_level_cells(self.h, lev, C.byref(n)), "mbg_level_cells")
+        return n.value
+
+    def set_state(self, lev, f, g):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        self._check(self.L.mbg_set_state(self.h, lev, _dp(f), _dp(g)), "mbg_set_state")
+
+    def get_state(self, lev):
+        n = self.ncells(lev)
+        f = np.empty(n * NQ)
+        g = np.empty(n * NQ)
+        self._check(self.L.mbg_get_state(self.h, lev, _dp(f), _dp(g)), "mbg_get_state")
+        return f, g
+
+    def get_macro(self, lev):
+        m = np.empty(self.ncells(lev) * NMACRO)
+        self._check(self.L.mbg_get_macro(self.h, lev, _dp(m)), "mbg_get_macro")
+        return m
+
+    def step(self, n=1):
+        self._check(self.L.mbg_step(self.h, n), "mbg_step")
+
+    def advance_level(self, lev):
+        self._check(self.L.mbg_advance_level(self.h, lev), "mbg_advance_level")
+
+    def fillpatch(self, lev):
+        self._check(self.L.mbg_fillpatch(self.h, lev), "mbg_fillpatch")
+
+    def average_down(self, crse_lev, ng):
+        self._check(self.L.mbg_average_down(self.h, crse_lev, ng), "mbg_average_down")
+
+    def eb_forces(self):
+        out = np.zeros(3)
+        self._check(self.L.mbg_eb_forces(self.h, _dp(out)), "mbg_eb_forces")
+        return out
+
+    def synchronize(self):
+        self._check(self.L.mbg_synchronize(self.h), "mbg_synchronize")
+
+    def launch_count(self):
+        return self.L.mbg_launch_count(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mbg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,734 @@
+// mbg_capi.cu -- the C ABI of include/marbles_gb300.h: context, level plans
+// and the subcycled step (Source/LBM.cpp:398-544 restated as launches).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/marbles_gb300.h"
+#include "mbg_kernels.h"
+#include "mbg_lowp.h"
+
+using namespace mbg;
+
+namespace {
+
+struct HBox {
+    int lo[3], hi[3];
+    int n(int d) const { return hi[d] - lo[d] + 1; }
+    long long vol() const { return (long long)n(0) * n(1) * n(2); }
+    long long gvol() const { return (long long)(n(0) + 6) * (n(1) + 6) * (n(2) + 6); }
+};
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+};
+
+struct Level {
+    std::vector<HBox> boxes;
+    std::vector<DevBox> hbox;
+    int dlo[3], dhi[3];
+    int G[3], nb[3];
+    std::vector<int> omap;
+    std::vector<uint8_t> hflags;
+    long long N = 0, NG = 0, NF = 0;
+    bool has_ghost = false;
+    // device
+    DevBox* d_box = nullptr;
+    int* d_omap = nullptr;
+    uint8_t* d_flags = nullptr;
+    double* f[2] = {nullptr, nullptr};
+    double* g[2] = {nullptr, nullptr};
+    double* fg[2] = {nullptr, nullptr};
+    double* gg[2] = {nullptr, nullptr};
+    double* md = nullptr;
+    double* gqc = nullptr;
+    Tile* d_tiles = nullptr;
+    int ntiles = 0;
+    GhostCell* d_ghost = nullptr;
+    GhostCell* d_ghost1 = nullptr;
+    long long nghost = 0, nghost1 = 0;
+    // coalescence of the next finer level onto this one (ng = 1 and ng = 0)
+    CoalesceCell* d_coal1 = nullptr;
+    long long ncoal1 = 0;
+    CoalesceCell* d_coal0 = nullptr;
+    long long ncoal0 = 0;
+    int cur = 0;
+    double dt = 1.0;
+    double dx[3], idx[3];
+    LevelPlan plan;
+    LowpLevel lowp;   // 16-bit storage form buffers (mbg_lowp.cu)
+};
+
+}  // namespace
+
+struct mbg_ctx {
+    mbg_params p;
+    cudaStream_t s = nullptr;
+    bool own_stream = false;
+    std::vector<Level> lv;
+    BCParams bc;
+    Lattice<double> lat;
+    std::string err;
+    long long launches = 0;
+    double* d_red = nullptr;   // small reduction scratch
+    double* d_out19 = nullptr;
+    size_t out19_n = 0;
+    std::vector<void*> allocs;
+};
+
+static std::string g_create_err;
+
+#define MBG_CUDA(call)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);               \
+            return MBG_ECUDA;                                                            \
+        }                                                                                \
+    } while (0)
+
+static mbg_status fail(mbg_ctx* ctx, mbg_status st, const std::string& m)
+{
+    ctx->err = m;
+    return st;
+}
+
+template <class T>
+static mbg_status dalloc(mbg_ctx* ctx, T** p, size_t n)
+{
+    *p = nullptr;
+    if (n == 0) return MBG_OK;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+    if (e != cudaSuccess) {
+        ctx->err = std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes: " + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? MBG_ENOMEM : MBG_ECUDA;
+    }
+    ctx->allocs.push_back(q);
+    *p = (T*)q;
+    return MBG_OK;
+}
+
+static Phys64 phys64(const mbg_ctx* ctx, const Level& L)
+{
+    Phys64 ph;
+    const mbg_params& p = ctx->p;
+    ph.mesh_speed = p.dx_outer / p.dt_outer;
+    ph.Rg = 28.96 / p.m_bar;
+    ph.cv = ph.Rg / (p.adiabatic_exponent - 1.0);
+    ph.nu = p.nu;
+    ph.alpha = p.alpha;
+    ph.dt = L.dt;
+    for (int d = 0; d < 3; ++d) ph.idx[d] = L.idx[d];
+    ph.small_num = std::numeric_limits<double>::epsilon() * 1e10;
+    ph.lat = ctx->lat;
+    return ph;
+}
+
+static bool wrap_host(const Level& L, const int per[3], int p[3])
+{
+    for (int d = 0; d < 3; ++d) {
+        if (p[d] < L.dlo[d] || p[d] > L.dhi[d]) {
+            if (!per[d]) return false;
+            const int len = L.dhi[d] - L.dlo[d] + 1;
+            p[d] = L.dlo[d] + (((p[d] - L.dlo[d]) % len) + len) % len;
+        }
+    }
+    return true;
+}
+
+static int owner_host(const Level& L, const int p[3])
+{
+    const int bi = (p[0] - L.dlo[0]) / L.G[0], bj = (p[1] - L.dlo[1]) / L.G[1], bk = (p[2] - L.dlo[2]) / L.G[2];
+    return L.omap[((size_t)bk * L.nb[1] + bj) * L.nb[0] + bi];
+}
+
+static void refresh_plan(mbg_ctx* ctx, Level& L)
+{
+    LevelView<double> v;
+    v.box = L.d_box;
+    v.nbox = (int)L.boxes.size();
+    for (int d = 0; d < 3; ++d) {
+        v.dlo[d] = L.dlo[d];
+        v.dhi[d] = L.dhi[d];
+        v.per[d] = ctx->p.is_periodic[d];
+        v.G[d] = L.G[d];
+        v.nb[d] = L.nb[d];
+    }
+    v.omap = L.d_omap;
+    v.N = L.N;
+    v.NG = L.NG;
+    v.flags = L.d_flags;
+    L.plan.view64 = v;
+    L.plan.tiles = L.d_tiles;
+    L.plan.ntiles = L.ntiles;
+    L.plan.ghost_list = L.d_ghost;
+    L.plan.nghost_cells = L.nghost;
+    L.plan.ghost_list1 = L.d_ghost1;
+    L.plan.nghost1 = L.nghost1;
+}
+
+extern "C" {
+
+mbg_status mbg_create(const mbg_params* params, void* cuda_stream, mbg_ctx** out)
+{
+    if (!params || !out) {
+        g_create_err = "mbg_create: null argument";
+        return MBG_EINVAL;
+    }
+    *out = nullptr;
+    const mbg_params& p = *params;
+    for (int d = 0; d < 3; ++d) {
+        if (p.n_cell[d] <= 0) { g_create_err = "mbg_create: n_cell must be positive"; return MBG_EINVAL; }
+        if (!(p.prob_hi[d] > p.prob_lo[d])) { g_create_err = "mbg_create: prob_hi must exceed prob_lo"; return MBG_EINVAL; }
+        const int codes[] = {0, 1, 2, 3, 5, 6, 7, 8};
+        for (int lh = 0; lh < 2; ++lh) {
+            const int c = lh ? p.bc_hi[d] : p.bc_lo[d];
+            if (std::find(std::begin(codes), std::end(codes), c) == std::end(codes)) {
+                g_create_err = "mbg_create: unknown boundary-condition code " + std::to_string(c);
+                return MBG_EINVAL;
+            }
+            if (p.is_periodic[d] && c != 0) {
+                g_create_err = "mbg_create: BC is periodic in direction " + std::to_string(d) + " but bc code is not 0";
+                return MBG_EINVAL;
+            }
+            if (!p.is_periodic[d] && c == 0) {
+                g_create_err = "mbg_create: BC is interior in direction " + std::to_string(d) + " but not periodic";
+                return MBG_EINVAL;
+            }
+            if (c == 3) {
+                g_create_err = "mbg_create: the pressure boundary condition (code 3) is not supported";
+                return MBG_EINVAL;
+            }
+        }
+    }
+    if (!(p.nu > 0) || !(p.alpha > 0) || !(p.dt_outer > 0) || !(p.m_bar > 0) || !(p.adiabatic_exponent > 1.0)) {
+        g_create_err = "mbg_create: nu, alpha, dt_outer, m_bar must be positive and adiabatic_exponent > 1";
+        return MBG_EINVAL;
+    }
+    if (p.vbc_dir < 0 || p.vbc_dir > 2 || p.vbc_normal_dir < 0 || p.vbc_normal_dir > 2 || p.vbc_tangential_dir < 0 ||
+        p.vbc_tangential_dir > 2) {
+        g_create_err = "mbg_create: velocity-BC directions must be 0, 1 or 2";
+        return MBG_EINVAL;
+    }
+    if (p.precision < 0 || p.precision > 2) {
+        g_create_err = "mbg_create: unknown precision form";
+        return MBG_EINVAL;
+    }
+    auto* ctx = new (std::nothrow) mbg_ctx();
+    if (!ctx) { g_create_err = "mbg_create: out of host memory"; return MBG_ENOMEM; }
+    ctx->p = p;
+    if (cuda_stream) {
+        ctx->s = (cudaStream_t)cuda_stream;
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&ctx->s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            g_create_err = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+            delete ctx;
+            return MBG_ECUDA;
+        }
+        ctx->own_stream = true;
+    }
+    ctx->lat = make_lattice<double>();
+    BCParams& bc = ctx->bc;
+    for (int d = 0; d < 3; ++d) { bc.bc[d] = p.bc_lo[d]; bc.bc[d + 3] = p.bc_hi[d]; }
+    bc.velbc = p.velbc_type;
+    bc.vbc_dir = p.vbc_dir;
+    bc.vbc_nd = p.vbc_normal_dir;
+    bc.vbc_td = p.vbc_tangential_dir;
+    bc.u_ref = p.vbc_u_ref;
+    bc.rho0 = p.vbc_initial_density;
+    bc.temp = p.vbc_initial_temperature;
+    bc.gamma = p.vbc_adiabatic_exponent;
+    bc.Rg = 28.96 / p.vbc_m_bar;
+    for (int d = 0; d < 3; ++d) {
+        bc.prob_lo[d] = p.prob_lo[d];
+        bc.prob_hi[d] = p.prob_hi[d];
+        bc.dx[d] = (p.prob_hi[d] - p.prob_lo[d]) / p.n_cell[d];
+    }
+    if (dalloc(ctx, &ctx->d_red, 8) != MBG_OK) {
+        g_create_err = ctx->err;
+        mbg_destroy(ctx);
+        return MBG_ENOMEM;
+    }
+    *out = ctx;
+    return MBG_OK;
+}
+
+void mbg_destroy(mbg_ctx* ctx)
+{
+    if (!ctx) return;
+    if (ctx->s) cudaStreamSynchronize(ctx->s);
+    for (void* q : ctx->allocs) cudaFree(q);
+    if (ctx->own_stream && ctx->s) cudaStreamDestroy(ctx->s);
+    delete ctx;
+}
+
+const char* mbg_last_error(const mbg_ctx* ctx)
+{
+    return ctx ? ctx->err.c_str() : g_create_err.c_str();
+}
+
+mbg_status mbg_level_cells(const mbg_ctx* ctx, int lev, long long* n)
+{
+    if (!ctx || !n) return MBG_EINVAL;
+    if (lev < 0 || lev >= (int)ctx->lv.size()) return MBG_ESTATE;
+    *n = ctx->lv[lev].N;
+    return MBG_OK;
+}
+
+long long mbg_launch_count(const mbg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, const uint8_t* flags)
+{
+    if (!ctx) return MBG_EINVAL;
+    if (lev != (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_define_level: levels must be defined in order 0, 1, ...");
+    if (nbox <= 0 || !lohi) return fail(ctx, MBG_EINVAL, "mbg_define_level: need at least one box");
+    const mbg_params& p = ctx->p;
+    Level L;
+    const int r = 1 << lev;
+    for (int d = 0; d < 3; ++d) {
+        L.dlo[d] = 0;
+        L.dhi[d] = p.n_cell[d] * r - 1;
+        L.dx[d] = (p.prob_hi[d] - p.prob_lo[d]) / (p.n_cell[d] * r);
+        L.idx[d] = 1.0 / L.dx[d];
+    }
+    L.dt = 1.0;
+    for (int l = 1; l <= lev; ++l) L.dt = L.dt / 2;
+    L.boxes.resize(nbox);
+    for (int n = 0; n < nbox; ++n) {
+        HBox& b = L.boxes[n];
+        for (int d = 0; d < 3; ++d) {
+            b.lo[d] = lohi[6 * n + d];
+            b.hi[d] = lohi[6 * n + 3 + d];
+            if (b.hi[d] < b.lo[d] || b.lo[d] < L.dlo[d] || b.hi[d] > L.dhi[d])
+                return fail(ctx, MBG_EINVAL, "mbg_define_level: box " + std::to_string(n) + " is empty or outside the domain");
+            if (b.n(d) > 32000) return fail(ctx, MBG_EINVAL, "mbg_define_level: box too long");
+        }
+    }
+    // owner map on gcd bins; also rejects overlapping boxes
+    for (int d = 0; d < 3; ++d) {
+        int g = L.dhi[d] - L.dlo[d] + 1;
+        for (const auto& b : L.boxes) {
+            g = std::gcd(g, b.lo[d] - L.dlo[d]);
+            g = std::gcd(g, b.hi[d] + 1 - L.dlo[d]);
+        }
+        L.G[d] = g > 0 ? g : 1;
+        L.nb[d] = (L.dhi[d] - L.dlo[d] + 1) / L.G[d];
+    }
+    L.omap.assign((size_t)L.nb[0] * L.nb[1] * L.nb[2], -1);
+    for (int n = 0; n < nbox; ++n) {
+        const HBox& b = L.boxes[n];
+        for (int k = b.lo[2] / L.G[2]; k <= b.hi[2] / L.G[2]; ++k)
+            for (int j = b.lo[1] / L.G[1]; j <= b.hi[1] / L.G[1]; ++j)
+                for (int i = b.lo[0] / L.G[0]; i <= b.hi[0] / L.G[0]; ++i) {
+                    int& o = L.omap[((size_t)k * L.nb[1] + j) * L.nb[0] + i];
+                    if (o >= 0) return fail(ctx, MBG_EINVAL, "mbg_define_level: boxes overlap");
+                    o = n;
+                }
+    }
+    if (lev == 0) {
+        long long cov = 0;
+        for (const auto& b : L.boxes) cov += b.vol();
+        long long dom = (long long)(L.dhi[0] + 1) * (L.dhi[1] + 1) * (L.dhi[2] + 1);
+        if (cov != dom) return fail(ctx, MBG_EINVAL, "mbg_define_level: level 0 boxes must cover the domain");
+    }
+    // per-box offsets and flags
+    L.hbox.resize(nbox);
+    long long voff = 0, foff = 0;
+    for (int n = 0; n < nbox; ++n) {
+        DevBox& B = L.hbox[n];
+        for (int d = 0; d < 3; ++d) { B.lo[d] = L.boxes[n].lo[d]; B.n[d] = L.boxes[n].n(d); }
+        B.voff = voff;
+        B.foff = foff;
+        B.goff = -1;
+        voff += L.boxes[n].vol();
+        foff += L.boxes[n].gvol();
+    }
+    L.N = voff;
+    L.NF = foff;
+    L.hflags.assign(foff, FL_FLUID);
+    if (flags) {
+        for (long long i = 0; i < foff; ++i) L.hflags[i] = flags[i] & (FL_FLUID | FL_EBB);
+    }
+    for (int n = 0; n < nbox; ++n) {
+        DevBox& B = L.hbox[n];
+        B.all_fluid = 1;
+        for (long long i = 0; i < L.boxes[n].gvol(); ++i)
+            if (!(L.hflags[B.foff + i] & FL_FLUID)) { B.all_fluid = 0; break; }
+    }
+    // coarse-fine ghost shell of fine levels
+    std::vector<GhostCell> ghosts, ghosts1;
+    if (lev > 0) {
+        Level& C = ctx->lv[lev - 1];
+        long long goff = 0;
+        for (int n = 0; n < nbox; ++n) {
+            const HBox& b = L.boxes[n];
+            bool any = false;
+            for (int z = -3; z < b.n(2) + 3; ++z)
+                for (int y = -3; y < b.n(1) + 3; ++y)
+                    for (int x = -3; x < b.n(0) + 3; ++x) {
+                        if (x >= 0 && y >= 0 && z >= 0 && x < b.n(0) && y < b.n(1) && z < b.n(2)) continue;
+                        int gp[3] = {b.lo[0] + x, b.lo[1] + y, b.lo[2] + z};
+                        if (!wrap_host(L, p.is_periodic, gp))
+                            return fail(ctx, MBG_EINVAL,
+                                        "mbg_define_level: fine level " + std::to_string(lev) +
+                                            " reaches a non-periodic domain boundary (unsupported)");
+                        if (owner_host(L, gp) >= 0) continue;
+                        // the interpolation stencil must lie in the coarse level's valid cells
+                        const int cp[3] = {gp[0] >> 1, gp[1] >> 1, gp[2] >> 1};
+                        for (int d = 0; d < 3; ++d)
+                            for (int s = -1; s <= 1; ++s) {
+                                int c[3] = {cp[0], cp[1], cp[2]};
+                                c[d] += s;
+                                if (!wrap_host(C, p.is_periodic, c) || owner_host(C, c) < 0)
+                                    return fail(ctx, MBG_EINVAL,
+                                                "mbg_define_level: level " + std::to_string(lev) +
+                                                    " is not properly nested in level " + std::to_string(lev - 1));
+                            }
+                        GhostCell gc;
+                        gc.box = n;
+                        gc.x = (short)x; gc.y = (short)y; gc.z = (short)z;
+                        gc.layer = (short)std::max({x < 0 ? -x : x - b.n(0) + 1, y < 0 ? -y : y - b.n(1) + 1,
+                                                    z < 0 ? -z : z - b.n(2) + 1, 0});
+                        ghosts.push_back(gc);
+                        if (gc.layer == 1) ghosts1.push_back(gc);
+                        any = true;
+                    }
+            if (any) {
+                L.hbox[n].goff = goff;
+                goff += b.gvol();
+            }
+        }
+        L.NG = goff;
+        L.has_ghost = goff > 0;
+        // cells of the uncovered shell also need their flags from the caller
+        // coalescence lists onto the coarse level (ascending box order, the
+        // last box whose grown coarsened box holds a cell wins)
+        for (int ng = 0; ng <= 1; ++ng) {
+            std::unordered_map<long long, int> win;
+            std::vector<long long> order;
+            for (int n = 0; n < nbox; ++n) {
+                const HBox& b = L.boxes[n];
+                if (b.lo[0] % 2 || b.lo[1] % 2 || b.lo[2] % 2 || b.n(0) % 2 || b.n(1) % 2 || b.n(2) % 2)
+                    return fail(ctx, MBG_EINVAL, "mbg_define_level: fine boxes must be aligned to the ratio 2");
+                for (int cz = b.lo[2] / 2 - ng; cz <= b.hi[2] / 2 + ng; ++cz)
+                    for (int cy = b.lo[1] / 2 - ng; cy <= b.hi[1] / 2 + ng; ++cy)
+                        for (int cx = b.lo[0] / 2 - ng; cx <= b.hi[0] / 2 + ng; ++cx) {
+                            int c[3] = {cx, cy, cz};
+                            if (cx < C.dlo[0] || cy < C.dlo[1] || cz < C.dlo[2] || cx > C.dhi[0] || cy > C.dhi[1] ||
+                                cz > C.dhi[2] || owner_host(C, c) < 0)
+                                return fail(ctx, MBG_EINVAL,
+                                            "mbg_define_level: coalescence region of level " + std::to_string(lev) +
+                                                " leaves the coarse level");
+                            const long long key = ((long long)cz * 65536 + cy) * 65536 + cx;
+                            auto it = win.find(key);
+                            if (it == win.end()) { win[key] = n; order.push_back(key); }
+                            else it->second = n;
+                        }
+            }
+            std::vector<CoalesceCell> cl;
+            cl.reserve(order.size());
+            for (long long key : order) {
+                const int cx = (int)(key % 65536), cy = (int)((key / 65536) % 65536), cz = (int)(key / 65536 / 65536);
+                int c[3] = {cx, cy, cz};
+                const int o = owner_host(C, c);
+                const int n = win[key];
+                CoalesceCell cc;
+                cc.cbox = o;
+                cc.fbox = n;
+                cc.cx = (short)(cx - C.boxes[o].lo[0]);
+                cc.cy = (short)(cy - C.boxes[o].lo[1]);
+                cc.cz = (short)(cz - C.boxes[o].lo[2]);
+                cc.fx = (short)(2 * cx - L.boxes[n].lo[0]);
+                cc.fy = (short)(2 * cy - L.boxes[n].lo[1]);
+                cc.fz = (short)(2 * cz - L.boxes[n].lo[2]);
+                cl.push_back(cc);
+                // flag the coarse cell
+                const DevBox& CB = C.hbox[o];
+                const long long fi = CB.foff + ((long long)(cc.cz + 3) * (CB.n[1] + 6) + (cc.cy + 3)) * (CB.n[0] + 6) + (cc.cx + 3);
+                C.hflags[fi] |= (uint8_t)(ng == 1 ? (uint8_t)FL_OVR : (uint8_t)FL_COV);
+            }
+            CoalesceCell** dst = ng ? &C.d_coal1 : &C.d_coal0;
+            long long* cnt = ng ? &C.ncoal1 : &C.ncoal0;
+            mbg_status st = dalloc(ctx, dst, cl.size());
+            if (st != MBG_OK) return st;
+            if (!cl.empty())
+                MBG_CUDA(cudaMemcpy(*dst, cl.data(), cl.size() * sizeof(CoalesceCell), cudaMemcpyHostToDevice));
+            *cnt = (long long)cl.size();
+        }
+        // re-upload the coarse flags with the coalescence bits
+        MBG_CUDA(cudaMemcpy(C.d_flags, C.hflags.data(), C.hflags.size(), cudaMemcpyHostToDevice));
+    }
+    // device allocations
+    mbg_status st;
+    if ((st = dalloc(ctx, &L.d_box, nbox)) != MBG_OK) return st;
+    MBG_CUDA(cudaMemcpy(L.d_box, L.hbox.data(), nbox * sizeof(DevBox), cudaMemcpyHostToDevice));
+    if ((st = dalloc(ctx, &L.d_omap, L.omap.size())) != MBG_OK) return st;
+    MBG_CUDA(cudaMemcpy(L.d_omap, L.omap.data(), L.omap.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if ((st = dalloc(ctx, &L.d_flags, L.hflags.size())) != MBG_OK) return st;
+    MBG_CUDA(cudaMemcpy(L.d_flags, L.hflags.data(), L.hflags.size(), cudaMemcpyHostToDevice));
+    std::vector<Tile> tiles;
+    for (int n = 0; n < nbox; ++n)
+        for (long long s = 0; s < L.boxes[n].vol(); s += TILE_CELLS) tiles.push_back(Tile{n, (int)s});
+    L.ntiles = (int)tiles.size();
+    if ((st = dalloc(ctx, &L.d_tiles, tiles.size())) != MBG_OK) return st;
+    MBG_CUDA(cudaMemcpy(L.d_tiles, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    L.nghost = (long long)ghosts.size();
+    L.nghost1 = (long long)ghosts1.size();
+    if ((st = dalloc(ctx, &L.d_ghost, ghosts.size())) != MBG_OK) return st;
+    if ((st = dalloc(ctx, &L.d_ghost1, ghosts1.size())) != MBG_OK) return st;
+    if (!ghosts.empty())
+        MBG_CUDA(cudaMemcpy(L.d_ghost, ghosts.data(), ghosts.size() * sizeof(GhostCell), cudaMemcpyHostToDevice));
+    if (!ghosts1.empty())
+        MBG_CUDA(cudaMemcpy(L.d_ghost1, ghosts1.data(), ghosts1.size() * sizeof(GhostCell), cudaMemcpyHostToDevice));
+    if (p.precision == MBG_FP64) {
+        for (int b = 0; b < 2; ++b) {
+            if ((st = dalloc(ctx, &L.f[b], (size_t)L.N * NQ)) != MBG_OK) return st;
+            if ((st = dalloc(ctx, &L.g[b], (size_t)L.N * NQ)) != MBG_OK) return st;
+            MBG_CUDA(cudaMemset(L.f[b], 0, (size_t)L.N * NQ * sizeof(double)));
+            MBG_CUDA(cudaMemset(L.g[b], 0, (size_t)L.N * NQ * sizeof(double)));
+            if (L.NG > 0) {
+                if ((st = dalloc(ctx, &L.fg[b], (size_t)L.NG * NQ)) != MBG_OK) return st;
+                if ((st = dalloc(ctx, &L.gg[b], (size_t)L.NG * NQ)) != MBG_OK) return st;
+                MBG_CUDA(cudaMemset(L.fg[b], 0, (size_t)L.NG * NQ * sizeof(double)));
+                MBG_CUDA(cudaMemset(L.gg[b], 0, (size_t)L.NG * NQ * sizeof(double)));
+            }
+        }
+        if ((st = dalloc(ctx, &L.md, (size_t)L.N * MD_NCOMP)) != MBG_OK) return st;
+        MBG_CUDA(cudaMemset(L.md, 0, (size_t)L.N * MD_NCOMP * sizeof(double)));
+        if (L.NG > 0) {
+            if ((st = dalloc(ctx, &L.gqc, (size_t)L.NG * 3)) != MBG_OK) return st;
+            MBG_CUDA(cudaMemset(L.gqc, 0, (size_t)L.NG * 3 * sizeof(double)));
+        }
+    }
+    ctx->lv.push_back(std::move(L));
+    Level& LL = ctx->lv.back();
+    refresh_plan(ctx, LL);
+    if (p.precision != MBG_FP64) {
+        mbg_status s2 = lowp_define(ctx->p, LL.plan, LL.hbox, LL.N, LL.NG, LL.lowp, ctx->err);
+        if (s2 != MBG_OK) return s2;
+    }
+    return MBG_OK;
+}
+
+mbg_status mbg_set_state(mbg_ctx* ctx, int lev, const double* f, const double* g)
+{
+    if (!ctx) return MBG_EINVAL;
+    if (lev < 0 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_set_state: level not defined");
+    Level& L = ctx->lv[lev];
+    if (ctx->p.precision != MBG_FP64) {
+        mbg_status s2 = lowp_set_state(L.lowp, L.plan, L.hbox, f, g, ctx->s, ctx->err);
+        ctx->launches += 2;
+        return s2;
+    }
+    long long off = 0;
+    for (size_t n = 0; n < L.boxes.size(); ++n) {
+        const long long vol = L.boxes[n].vol();
+        const long long voff = L.hbox[n].voff;
+        if (f)
+            MBG_CUDA(cudaMemcpy2DAsync(L.f[L.cur] + voff, L.N * sizeof(double), f + off * NQ, vol * sizeof(double),
+                                       vol * sizeof(double), NQ, cudaMemcpyHostToDevice, ctx->s));
+        if (g)
+            MBG_CUDA(cudaMemcpy2DAsync(L.g[L.cur] + voff, L.N * sizeof(double), g + off * NQ, vol * sizeof(double),
+                                       vol * sizeof(double), NQ, cudaMemcpyHostToDevice, ctx->s));
+        off += vol;
+    }
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+mbg_status mbg_get_state(mbg_ctx* ctx, int lev, double* f, double* g)
+{
+    if (!ctx) return MBG_EINVAL;
+    if (lev < 0 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_get_state: level not defined");
+    Level& L = ctx->lv[lev];
+    if (ctx->p.precision != MBG_FP64) {
+        mbg_status s2 = lowp_get_state(L.lowp, L.plan, L.hbox, f, g, ctx->s, ctx->err);
+        ctx->launches += 2;
+        return s2;
+    }
+    long long off = 0;
+    for (size_t n = 0; n < L.boxes.size(); ++n) {
+        const long long vol = L.boxes[n].vol();
+        const long long voff = L.hbox[n].voff;
+        if (f)
+            MBG_CUDA(cudaMemcpy2DAsync(f + off * NQ, vol * sizeof(double), L.f[L.cur] + voff, L.N * sizeof(double),
+                                       vol * sizeof(double), NQ, cudaMemcpyDeviceToHost, ctx->s));
+        if (g)
+            MBG_CUDA(cudaMemcpy2DAsync(g + off * NQ, vol * sizeof(double), L.g[L.cur] + voff, L.N * sizeof(double),
+                                       vol * sizeof(double), NQ, cudaMemcpyDeviceToHost, ctx->s));
+        off += vol;
+    }
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+mbg_status mbg_get_macro(mbg_ctx* ctx, int lev, double* macro)
+{
+    if (!ctx || !macro) return MBG_EINVAL;
+    if (lev < 0 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_get_macro: level not defined");
+    Level& L = ctx->lv[lev];
+    const size_t need = (size_t)L.N * 19;
+    if (ctx->out19_n < need) {
+        mbg_status st = dalloc(ctx, &ctx->d_out19, need);
+        if (st != MBG_OK) return st;
+        ctx->out19_n = need;
+    }
+    if (ctx->p.precision != MBG_FP64) {
+        mbg_status s2 = lowp_macro(L.lowp, L.plan, ctx->d_out19, ctx->s, ctx->err);
+        if (s2 != MBG_OK) return s2;
+    } else {
+        launch_macro_local(L.plan, phys64(ctx, L), L.f[L.cur], L.g[L.cur], ctx->d_out19, ctx->s);
+    }
+    ctx->launches++;
+    MBG_CUDA(cudaGetLastError());
+    MBG_CUDA(cudaMemcpyAsync(macro, ctx->d_out19, need * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+}  // extern "C"
+
+// ---- the step ---------------------------------------------------------------
+static mbg_status explode(mbg_ctx* ctx, int lev)
+{
+    Level& F = ctx->lv[lev];
+    Level& C = ctx->lv[lev - 1];
+    if (ctx->p.precision != MBG_FP64) {
+        lowp_explode(F.lowp, F.plan, C.lowp, C.plan, ctx->s);
+    } else {
+        launch_explode(F.plan, C.plan, C.f[C.cur], C.g[C.cur], F.fg[F.cur], F.gg[F.cur], ctx->s);
+    }
+    ctx->launches++;
+    MBG_CUDA(cudaGetLastError());
+    return MBG_OK;
+}
+
+static mbg_status advance(mbg_ctx* ctx, int lev)
+{
+    Level& L = ctx->lv[lev];
+    const bool has_finer = lev + 1 < (int)ctx->lv.size();
+    if (ctx->p.precision != MBG_FP64) {
+        const LowpLevel* fine = has_finer ? &ctx->lv[lev + 1].lowp : nullptr;
+        const LevelPlan* fplan = has_finer ? &ctx->lv[lev + 1].plan : nullptr;
+        int nl = lowp_advance(ctx->p, ctx->bc, L.lowp, L.plan, L.dt, L.idx, has_finer ? L.d_coal1 : nullptr,
+                              has_finer ? L.ncoal1 : 0, fine, fplan, ctx->s);
+        ctx->launches += nl;
+        MBG_CUDA(cudaGetLastError());
+        return MBG_OK;
+    }
+    const Phys64 ph = phys64(ctx, L);
+    const int A = L.cur, Bf = 1 - L.cur;
+    if (has_finer) {
+        Level& F = ctx->lv[lev + 1];
+        launch_coalesce(L.plan, F.plan, ctx->bc, ph, L.d_coal1, L.ncoal1, F.f[F.cur], F.g[F.cur], F.fg[F.cur],
+                        F.gg[F.cur], L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], 0, ctx->s);
+        ctx->launches++;
+    }
+    if (L.NG > 0) {
+        launch_ghost_stream(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.fg[Bf], L.gg[Bf], ctx->s);
+        launch_ghost_moments(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.gqc, ctx->s);
+        ctx->launches += 2;
+    }
+    launch_moments(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], L.md, ctx->s);
+    launch_collide(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], L.md, L.gqc, ctx->s);
+    ctx->launches += 2;
+    MBG_CUDA(cudaGetLastError());
+    L.cur = Bf;
+    return MBG_OK;
+}
+
+static mbg_status time_step(mbg_ctx* ctx, int lev)
+{
+    mbg_status st;
+    if (lev + 1 < (int)ctx->lv.size()) {
+        if ((st = explode(ctx, lev + 1)) != MBG_OK) return st;
+        for (int i = 1; i <= 2; ++i)
+            if ((st = time_step(ctx, lev + 1)) != MBG_OK) return st;
+    }
+    return advance(ctx, lev);
+}
+
+extern "C" {
+
+mbg_status mbg_step(mbg_ctx* ctx, int nsteps)
+{
+    if (!ctx) return MBG_EINVAL;
+    if (ctx->lv.empty()) return fail(ctx, MBG_ESTATE, "mbg_step: no level defined");
+    for (int i = 0; i < nsteps; ++i) {
+        mbg_status st = time_step(ctx, 0);
+        if (st != MBG_OK) return st;
+    }
+    return MBG_OK;
+}
+
+mbg_status mbg_advance_level(mbg_ctx* ctx, int lev)
+{
+    if (!ctx) return MBG_EINVAL;
+    if (lev < 0 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_advance_level: level not defined");
+    return advance(ctx, lev);
+}
+
+mbg_status mbg_fillpatch(mbg_ctx* ctx, int lev)
+{
+    if (!ctx) return MBG_EINVAL;
+    if (lev < 0 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_fillpatch: level not defined");
+    if (lev == 0) return MBG_OK;  // level-0 ghosts are never stored: pulls read neighbours and BCs directly
+    return explode(ctx, lev);
+}
+
+mbg_status mbg_average_down(mbg_ctx* ctx, int crse_lev, int crse_ng)
+{
+    if (!ctx) return MBG_EINVAL;
+    if (crse_lev < 0 || crse_lev + 1 >= (int)ctx->lv.size())
+        return fail(ctx, MBG_ESTATE, "mbg_average_down: needs levels crse_lev and crse_lev+1");
+    if (crse_ng != 0 && crse_ng != 1) return fail(ctx, MBG_EINVAL, "mbg_average_down: crse_ng must be 0 or 1");
+    Level& C = ctx->lv[crse_lev];
+    Level& F = ctx->lv[crse_lev + 1];
+    const CoalesceCell* list = crse_ng ? C.d_coal1 : C.d_coal0;
+    const long long n = crse_ng ? C.ncoal1 : C.ncoal0;
+    if (ctx->p.precision != MBG_FP64) {
+        lowp_average_down(C.lowp, C.plan, F.lowp, F.plan, list, n, ctx->s);
+    } else {
+        launch_coalesce(C.plan, F.plan, ctx->bc, phys64(ctx, C), list, n, F.f[F.cur], F.g[F.cur], F.fg[F.cur],
+                        F.gg[F.cur], C.f[C.cur], C.g[C.cur], C.fg[C.cur], C.gg[C.cur], C.f[C.cur], C.g[C.cur], 1,
+                        ctx->s);
+    }
+    ctx->launches++;
+    MBG_CUDA(cudaGetLastError());
+    return MBG_OK;
+}
+
+mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3])
+{
+    if (!ctx || !out) return MBG_EINVAL;
+    if (ctx->p.precision != MBG_FP64) return fail(ctx, MBG_EINVAL, "mbg_eb_forces: FP64 form only");
+    MBG_CUDA(cudaMemsetAsync(ctx->d_red, 0, 3 * sizeof(double), ctx->s));
+    for (auto& L : ctx->lv) {
+        launch_eb_forces(L.plan, L.f[L.cur], L.fg[L.cur], ctx->d_red, ctx->s);
+        ctx->launches++;
+    }
+    MBG_CUDA(cudaGetLastError());
+    MBG_CUDA(cudaMemcpyAsync(out, ctx->d_red, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+mbg_status mbg_synchronize(mbg_ctx* ctx)
+{
+    if (!ctx) return MBG_EINVAL;
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    MBG_CUDA(cudaGetLastError());
+    return MBG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,88 @@
+// mbg_kernels.h -- plan structures shared by the host orchestration
+// (mbg_capi.cu) and the kernel files, and the launcher declarations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mbg_level.cuh"
+
+namespace mbg {
+
+constexpr int TILE_CELLS = 128;   // cells (threads) per CTA in the per-cell passes
+
+// scratch macro-field components of the FP64 form
+enum {
+    MD_RHO = 0, MD_U, MD_V, MD_W, MD_TRE, MD_PXX, MD_PYY, MD_PZZ, MD_PXY, MD_PXZ, MD_PYZ,
+    MD_QX, MD_QY, MD_QZ, MD_T, MD_QCX, MD_QCY, MD_QCZ, MD_NCOMP
+};
+
+enum : uint8_t { FL_COV = 8 };   // covered by a finer level (EB force mask)
+
+struct Tile {
+    int box;
+    int start;   // first cell (linear index inside the box)
+};
+
+struct GhostCell {
+    int box;
+    short x, y, z;   // box-local position in the grown fab (-3 .. n+2)
+    short layer;     // Chebyshev distance to the box
+};
+
+struct CoalesceCell {
+    int cbox;             // coarse box holding the cell
+    int fbox;             // fine box whose average is kept (last writer)
+    short cx, cy, cz;     // coarse box-local position
+    short fx, fy, fz;     // first child, fine box-local position
+};
+
+struct Phys64 {
+    double mesh_speed, Rg, cv, nu, alpha, dt;
+    double idx[3];
+    double small_num;
+    Lattice<double> lat;
+};
+
+struct Phys32 {
+    float mesh_speed, Rg, cv, nu, alpha, dt;
+    float idx[3];
+    float small_num;
+    Lattice<float> lat;
+    float frest[NQ], grest[NQ];   // rest-state equilibria (shift of the storage)
+    float fscale, gscale;         // storage = (value - rest) / scale
+    float inv_fscale, inv_gscale;
+};
+
+struct LevelPlan {
+    LevelView<double> view64;
+    const Tile* tiles = nullptr;
+    int ntiles = 0;
+    const GhostCell* ghost_list = nullptr;   // all uncovered ghost cells
+    long long nghost_cells = 0;
+    const GhostCell* ghost_list1 = nullptr;  // first ghost layer only
+    long long nghost1 = 0;
+};
+
+// FP64 form (mbg_fp64.cu)
+void launch_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
+                    const double* fAg, const double* gAg, const double* fB, const double* gB, double* md,
+                    cudaStream_t s);
+void launch_collide(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
+                    const double* fAg, const double* gAg, double* fB, double* gB, const double* md,
+                    const double* gqc, cudaStream_t s);
+void launch_ghost_stream(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA,
+                         const double* gA, const double* fAg, const double* gAg, double* fBg, double* gBg,
+                         cudaStream_t s);
+void launch_ghost_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA,
+                          const double* gA, const double* fAg, const double* gAg, double* gqc, cudaStream_t s);
+void launch_explode(const LevelPlan& fine, const LevelPlan& crse, const double* fc, const double* gc, double* fg,
+                    double* gg, cudaStream_t s);
+void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParams& P, const Phys64& ph,
+                     const CoalesceCell* list, long long n, const double* ff, const double* gf, const double* ffg,
+                     const double* gfg, const double* fcA, const double* gcA, const double* fcAg,
+                     const double* gcAg, double* fcB, double* gcB, int into_state, cudaStream_t s);
+void launch_macro_local(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, double* out19,
+                        cudaStream_t s);
+void launch_eb_forces(const LevelPlan& lp, const double* f, const double* fg, double* out3, cudaStream_t s);
+
+}  // namespace mbg

@@ -1,0 +1,76 @@
+"""The oracle against the reference's own known answers (CPU only)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_stencil_tables_match_reference_source():
+    """Direction order, bounce/mirror tables and weights of Source/Stencil.H."""
+    ref = json.load(open(os.path.join(GOLD, "stencil_d3q27.json")))
+    ev, w, bounce, bx, by, bz = O.stencil_tables()
+    assert ev.tolist() == ref["ev"]
+    assert bounce.tolist() == ref["bounce_dirs"]
+    assert bx.tolist() == ref["bounce_Xdir"]
+    assert by.tolist() == ref["bounce_Ydir"]
+    assert bz.tolist() == ref["bounce_Zdir"]
+    # check_stencil (Source/Stencil.cpp:5-61)
+    for q in range(27):
+        assert (ev[q] + ev[bounce[q]] == 0).all()
+        s = int(np.abs(ev[q]).sum())
+        target = {0: 8 / 27, 1: 2 / 27, 2: 1 / 54, 3: 1 / 216}[s]
+        assert abs(w[q] - target) <= np.finfo(float).eps * 1e10
+    WSC1, WFCC1, WBCC1 = 2.0 / 27.0, 1.0 / 54.0, 1.0 / 216.0
+    assert w[0] == 1.0 - (6.0 * WSC1 + 12.0 * WFCC1 + 8.0 * WBCC1)
+
+
+def _notebook_case(name):
+    nb = json.load(open(os.path.join(GOLD, "notebook_runs.json")))[name]
+    inp = nb["inputs"]
+    p = O.default_params()
+    p.n_cell[:] = inp["n_cell"]
+    p.prob_lo[:] = inp["prob_lo"]
+    p.prob_hi[:] = inp["prob_hi"]
+    p.max_grid_size = 200
+    p.nu = inp["nu"]
+    p.alpha = inp.get("alpha", inp["nu"])
+    for pre in ("", "ic_"):
+        setattr(p, pre + "initial_temperature", inp["initial_temperature"])
+        setattr(p, pre + "adiabatic_exponent", inp["adiabatic_exponent"])
+    p.m_bar = inp["mean_molecular_mass"]
+    p.ic_m_bar = inp["mean_molecular_mass"]
+    p.ic_wave_length = inp["wave_length"]
+    p.ic_type = O.IC_TYPES[name]
+    boxes = O.chop_domain(inp["n_cell"], 200)
+    return nb, O.Oracle(p, [boxes])
+
+
+def test_viscosity_test_initial_max_velocity_exact():
+    nb, o = _notebook_case("viscosity_test")
+    o.init()
+    m = o.get_macro(0).reshape(19, -1)
+    assert m[1].max() == nb["ux_max"][0]
+
+
+@pytest.mark.slow
+def test_viscosity_test_decay_matches_recorded_run():
+    """uxMax after 5000 steps of Tests/test_files/viscosity_test against the
+    value recorded from the reference (viscosity_tester.ipynb)."""
+    nb, o = _notebook_case("viscosity_test")
+    o.init()
+    o.step(nb["interval"])
+    m = o.get_macro(0).reshape(19, -1)
+    rel = abs(m[1].max() / nb["ux_max"][1] - 1.0)
+    assert rel < 1e-9, rel
+
+
+def test_thermaldiffusivity_initial_max_temperature_exact():
+    nb, o = _notebook_case("thermaldiffusivity_test")
+    o.init()
+    m = o.get_macro(0).reshape(19, -1)
+    assert abs(m[18].max() / nb["t_max"][0] - 1.0) < 1e-15

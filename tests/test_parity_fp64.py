@@ -1,0 +1,151 @@
+"""FP64 CUDA path against the oracle on the same inputs (GPU).
+
+Both start from the oracle's initial state (same box layout, same flags);
+after the same number of coarse steps the populations f, g and the macro
+fields rho, u, T must agree to 1e-12 relative (the FP64 form compiles with
+-fmad=false and keeps the reference's operand order, so they are normally
+bit-identical).
+"""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-12
+
+
+def _gpu_from_oracle(o, p, levels, precision=0):
+    import marbles_gb300 as M
+    ctx = M.Context(cases.mbg_params_from(p, precision))
+    for lev, b in enumerate(levels):
+        ctx.define_level(lev, b, o.get_grown_flags(lev))
+    for lev in range(len(levels)):
+        f, g = o.get_state(lev)
+        ctx.set_state(lev, f, g)
+    return ctx
+
+
+def _rel(a, b):
+    scale = np.max(np.abs(b))
+    return float(np.max(np.abs(a - b)) / scale) if scale > 0 else float(np.max(np.abs(a - b)))
+
+
+def _compare(ctx, o, nlev, rtol=RTOL):
+    worst = 0.0
+    for lev in range(nlev):
+        fg, gg = ctx.get_state(lev)
+        fo, go = o.get_state(lev)
+        assert np.isfinite(fg).all() and np.isfinite(gg).all()
+        worst = max(worst, _rel(fg, fo), _rel(gg, go))
+        mg = ctx.get_macro(lev).reshape(-1)
+        mo = o.get_macro(lev).reshape(-1)
+        nb = o.levels[lev]
+        # per box [19][cells]: compare rho (0), u (1..3), T (18)
+        off = 0
+        for b in nb:
+            vol = int(np.prod(b[3:] - b[:3] + 1))
+            a = mg[off:off + 19 * vol].reshape(19, vol)
+            r = mo[off:off + 19 * vol].reshape(19, vol)
+            for c in (0, 1, 2, 3, 18):
+                worst = max(worst, _rel(a[c], r[c]))
+            off += 19 * vol
+    assert worst <= rtol, worst
+    return worst
+
+
+def test_taylor_green_64_200_steps():
+    """Taylor-Green 64^3 periodic, 8 boxes of 32^3, 200 steps."""
+    p, levels = cases.taylor_green(64, 32)
+    o = cases.run_oracle(p, levels, 0)
+    ctx = _gpu_from_oracle(o, p, levels)
+    ctx.step(200)
+    o.step(200)
+    _compare(ctx, o, 1)
+
+
+def test_taylor_green_uneven_boxes():
+    """40^3 chopped by 16 gives 24/16 boxes: cross-box pulls of unequal boxes."""
+    p, levels = cases.taylor_green(40, 16)
+    o = cases.run_oracle(p, levels, 0)
+    ctx = _gpu_from_oracle(o, p, levels)
+    ctx.step(10)
+    o.step(10)
+    _compare(ctx, o, 1)
+
+
+def test_single_box_periodic_self_wrap():
+    """One box whose periodic images are itself (FillBoundary onto self)."""
+    p, levels = cases.taylor_green(16, 32)
+    o = cases.run_oracle(p, levels, 0)
+    ctx = _gpu_from_oracle(o, p, levels)
+    ctx.step(12)
+    o.step(12)
+    _compare(ctx, o, 1)
+
+
+def test_sphere_inflow_outflow_single_level():
+    """EB sphere, velocity inflow x-lo, outflow x-hi, periodic y/z."""
+    p, levels = cases.sphere_channel(64, 32, 32, radius=6.0, center=(20.0, 16.0, 16.0), mgs=16)
+    o = cases.run_oracle(p, levels, 0)
+    ctx = _gpu_from_oracle(o, p, levels)
+    ctx.step(20)
+    o.step(20)
+    _compare(ctx, o, 1)
+
+
+@pytest.mark.parametrize("bc_lo,bc_hi", [((2, 1, 0), (5, 1, 0)), ((2, 7, 0), (5, 7, 0)),
+                                         ((1, 1, 1), (1, 1, 1)), ((2, 6, 8), (5, 6, 8))])
+def test_wall_boundaries(bc_lo, bc_hi):
+    """No-slip and slip walls, including edges and corners of walls."""
+    p, levels = cases.sphere_channel(32, 24, 16, radius=4.0, center=(12.0, 12.0, 8.0), mgs=16,
+                                     bc_lo=bc_lo, bc_hi=bc_hi)
+    o = cases.run_oracle(p, levels, 0)
+    ctx = _gpu_from_oracle(o, p, levels)
+    ctx.step(8)
+    o.step(8)
+    _compare(ctx, o, 1)
+
+
+def test_gaussian_pulse_two_levels():
+    """Explosion, subcycling and coalescence on a small two-level pulse."""
+    p, levels = cases.gaussian_pulse(nc=32, fine_lo=8, fine_hi=23, mgs=16, width=3.0)
+    o = cases.run_oracle(p, levels, 0)
+    ctx = _gpu_from_oracle(o, p, levels)
+    ctx.step(6)
+    o.step(6)
+    _compare(ctx, o, 2)
+
+
+def test_sphere_three_levels():
+    """Three levels around an EB sphere with inflow/outflow on level 0."""
+    p, levels = cases.sphere_channel(64, 32, 32, radius=5.0, center=(24.0, 16.0, 16.0), mgs=16, levels=3)
+    o = cases.run_oracle(p, levels, 0)
+    ctx = _gpu_from_oracle(o, p, levels)
+    ctx.step(3)
+    o.step(3)
+    _compare(ctx, o, 3)
+
+
+def test_eb_forces_match():
+    p, levels = cases.sphere_channel(48, 24, 24, radius=5.0, center=(16.0, 12.0, 12.0), mgs=16, levels=2)
+    o = cases.run_oracle(p, levels, 0)
+    ctx = _gpu_from_oracle(o, p, levels)
+    ctx.step(4)
+    o.step(4)
+    a, b = ctx.eb_forces(), o.eb_forces()
+    assert np.allclose(a, b, rtol=1e-11, atol=1e-13), (a, b)
+
+
+def test_average_down_entry_point():
+    """mbg_average_down (ng = 0 and 1) against the oracle's state after one step."""
+    p, levels = cases.gaussian_pulse(nc=32, fine_lo=8, fine_hi=23, mgs=16, width=3.0)
+    o = cases.run_oracle(p, levels, 1)
+    ctx = _gpu_from_oracle(o, p, levels)
+    # the oracle's state after a step already satisfies the coalescence; the
+    # entry point must leave covered cells equal to the fine averages
+    ctx.average_down(0, 0)
+    fg, gg = ctx.get_state(0)
+    fo, go = o.get_state(0)
+    assert _rel(fg, fo) <= RTOL and _rel(gg, go) <= RTOL
