@@ -1,0 +1,320 @@
+"""Benchmark of the MARBLES level step on GB300 (one JSON line on rank 0).
+
+Workload: the two-level AMR Gaussian pulse -- coarse 128^3 periodic, fine
+level (ratio 2) over the central 64^3 coarse cells (128^3 fine cells),
+max_grid_size 32, blocking factor 8, nu = 0.01, rho = 1 + 0.01 exp(-r^2 / 2 8^2),
+u = 0, T = 1/3; each coarse step advances the coarse level once and the fine
+level twice (6.29 M cell-updates).  Inputs are synthetic (analytic IC).
+
+Metric: MLUPS (million fluid cell-updates per second, fine substeps
+counted), device-timed with CUDA events on the library's stream over K
+coarse steps after W warm-up steps; the state (1.8 GB in FP64) is far larger
+than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp64|fp16|bf16|all]
+  python bench.py --impl reference ...     # the CPU oracle on the host cores
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+BYTES_PER_CELL = {"fp64": 865, "fp16": 217, "bf16": 217}   # read + write f, g, one flag byte
+PRECISION = {"fp64": 0, "fp16": 1, "bf16": 2}
+WORKLOAD = ("two-level AMR Gaussian pulse: coarse 128^3 periodic + fine 128^3 (ratio 2 over the central "
+            "64^3 coarse cells), max_grid_size 32, blocking_factor 8, nu 0.01, D3Q27 f+g")
+
+
+WORKLOADS = {
+    "pulse128": dict(nc=128, lo=32, hi=96, mgs=32, width=8.0),
+    # small case of the same kernels for profiler captures (226 MB FP64 state)
+    "pulse64": dict(nc=64, lo=16, hi=48, mgs=32, width=4.0),
+}
+_WL = ["pulse128"]
+
+
+def inputs_text():
+    import inputs
+    return inputs.pulse(**WORKLOADS[_WL[0]])
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "fallback": True}
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        self.f = tempfile.TemporaryFile(mode="w+")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        if not self.p:
+            return None
+        self.f.seek(0)
+        sm, smax, reasons = [], 0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f:
+            v = [x.strip() for x in line.split(",")]
+            if len(v) < 7:
+                continue
+            try:
+                sm.append(float(v[0]))
+                smax = max(smax, float(v[1]))
+            except ValueError:
+                continue
+            for n, x in zip(names, v[3:7]):
+                if x.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cell_updates_per_step(ctx, nlev):
+    return sum(ctx.ncells(l) * (2 ** l) for l in range(nlev))
+
+
+def run_form(form, steps, warmup, device_index):
+    import numpy as np
+    import torch
+    import marbles_gb300 as M
+
+    d = M.LBM(inputs_text(), ["lbm.precision=" + form])
+    ctx = d.init()
+    nlev = d.num_levels()
+    cups = cell_updates_per_step(ctx, nlev)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    for _ in range(warmup):
+        ctx.step(1)
+    ctx.synchronize()
+    ctx.set_timing(True)
+    n0 = ctx.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(device_index) as clk:
+        ctx.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            ctx.step(1)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = ctx.launch_count() - n0
+    timing = ctx.timing()
+    ctx.set_timing(False)
+    res = {"form": form, "ms_per_step": ms / steps, "mlups": cups * steps / (ms * 1e-3) / 1e6,
+           "cell_updates_per_step": cups, "gpu_launches": launches,
+           "kernels": {k: {"launches": n, "ms": t} for k, (n, t) in timing.items() if n},
+           "clocks": clk.summary()}
+    # end to end through the C ABI with pinned host buffers: upload of the
+    # state, K steps each followed by the EB-force read-back (the reference
+    # computes it every step), download of the state
+    host = []
+    for lev in range(nlev):
+        n = ctx.ncells(lev) * M.NQ
+        f = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        g = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        host.append((f, g))
+    import ctypes as C
+    dp = C.POINTER(C.c_double)
+    lib = M.lib()
+    for lev, (f, g) in enumerate(host):
+        ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+    forces = torch.zeros(3, dtype=torch.float64, pin_memory=True)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for lev, (f, g) in enumerate(host):
+        ctx._check(lib.mbg_set_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
+    for _ in range(steps):
+        ctx.step(1)
+        ctx._check(lib.mbg_eb_forces(ctx.h, C.cast(forces.data_ptr(), dp)), "forces") if form == "fp64" else None
+    for lev, (f, g) in enumerate(host):
+        ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+    e1.record(stream)
+    e1.synchronize()
+    wall = time.perf_counter() - t0
+    state_bytes = sum(2 * f.numel() * 8 for f, _ in host)
+    res["e2e"] = {"value": cups * steps / wall / 1e6, "unit": "MLUPS",
+                  "h2d_bytes_per_step": state_bytes / steps,
+                  "d2h_bytes_per_step": state_bytes / steps + (24 if form == "fp64" else 0),
+                  "wall_s": wall, "device_ms": e0.elapsed_time(e1)}
+    finite = True
+    for lev, (f, g) in enumerate(host):
+        finite &= bool(torch.isfinite(f).all()) and bool(torch.isfinite(g).all())
+    res["state_finite"] = finite
+    d.close()
+    return res
+
+
+def roofline(res, form):
+    pk = peaks()
+    k = max(res["kernels"].items(), key=lambda kv: kv[1]["ms"])
+    name, kv = k
+    # algorithmic bytes per launch: per-cell figure x cells the launch updates
+    per_cell = BYTES_PER_CELL[form]
+    cells = res["cell_updates_per_step"] * res["kernels_steps"]
+    if name == "k_moments":
+        per_cell = 432 + 1 if form == "fp64" else per_cell
+    achieved = per_cell * cells / (kv["ms"] * 1e-3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get(form, {}).get(name)
+    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if not pk.get("fallback") else "fallback",
+            "bytes_per_cell": per_cell}
+
+
+def cpu_baseline(sample_steps=1):
+    """The FP64 oracle (port of the reference step) on the host cores, on a
+    bounded sample: initialisation excluded, sample_steps coarse steps."""
+    import cases
+    p, levels = cases.gaussian_pulse()
+    p.nthreads = os.cpu_count() or 1
+    from oracle import oracle as O
+    o = O.Oracle(p, levels)
+    o.init()
+    t = time.perf_counter()
+    o.step(sample_steps)
+    dt = time.perf_counter() - t
+    cups = sum(o.ncells(l) * 2 ** l for l in range(len(levels)))
+    return {"value": cups * sample_steps / dt / 1e6, "unit": "MLUPS", "cores": p.nthreads, "kind": "port",
+            "sample": "%d coarse step(s) of the full workload (%d cell-updates each), init excluded"
+                      % (sample_steps, cups)}
+
+
+def dist_setup(n):
+    if n <= 1:
+        return 0, 1
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", n))
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    dist.init_process_group("nccl", rank=rank, world_size=world)
+    return rank, world
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="all")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="pulse128", choices=sorted(WORKLOADS))
+    a = ap.parse_args()
+    _WL[0] = a.workload
+    a.warmup = max(a.warmup, 3)
+    rank, world = dist_setup(a.gpus)
+
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        # the reference itself cannot be built here (its AMReX submodule is
+        # absent); its CPU path is timed through the oracle port
+        import cases
+        from oracle import oracle as O
+        p, levels = cases.gaussian_pulse()
+        p.nthreads = os.cpu_count() or 1
+        o = O.Oracle(p, levels)
+        o.init()
+        o.step(a.warmup)
+        t = time.perf_counter()
+        o.step(a.steps)
+        dt = time.perf_counter() - t
+        cups = sum(o.ncells(l) * 2 ** l for l in range(len(levels)))
+        v = cups * a.steps / dt / 1e6
+        print(json.dumps({
+            "impl": "reference", "metric": "MLUPS", "value": v, "unit": "MLUPS", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": dt / a.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": "fp64 CPU", "parallelism": "host threads"},
+            "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": p.nthreads, "kind": "port",
+                             "sample": "%d coarse steps of the full workload" % a.steps},
+            "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    forms = ["fp64", "fp16", "bf16"] if a.form == "all" else a.form.split(",")
+    results = {}
+    for form in forms:
+        try:
+            if world > 1:
+                torch.distributed.barrier()
+            r = run_form(form, a.steps, a.warmup, dev)
+            r["kernels_steps"] = a.steps
+            if world > 1:
+                t = torch.tensor([r["ms_per_step"]], device="cuda")
+                torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+                r["ms_per_step"] = float(t.item())
+                r["mlups"] = r["cell_updates_per_step"] / (r["ms_per_step"] * 1e-3) / 1e6 * world
+            r["roofline"] = roofline(r, form)
+            results[form] = r
+        except Exception as ex:  # a form that is not built yet is reported, not fatal
+            results[form] = {"error": str(ex)[:300]}
+    if rank != 0:
+        return
+    head = next((f for f in ("fp16", "bf16", "fp64") if f in results and "mlups" in results[f]), None)
+    if head is None:
+        print(json.dumps({"metric": "MLUPS", "value": None, "error": results}))
+        sys.exit(1)
+    h = results[head]
+    line = {
+        "metric": "MLUPS", "value": h["mlups"], "unit": "MLUPS", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD if a.workload == "pulse128" else a.workload, "form": head, "l2": "state larger than L2 (no flush needed)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": h["roofline"], "e2e": h["e2e"], "gpu_launches": h["gpu_launches"], "clocks": h["clocks"],
+        "forms": {f: {k: v for k, v in r.items() if k not in ("kernels_steps",)} for f, r in results.items()},
+    }
+    if not a.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = cpu_baseline()
+        except Exception as ex:
+            line["cpu_baseline"] = {"error": str(ex)[:200]}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -156,6 +156,66 @@ mbg_status mbg_synchronize(mbg_ctx* ctx);
 /* Number of kernel launches issued by the context since creation. */
 long long mbg_launch_count(const mbg_ctx* ctx);
 
+/* The CUDA stream every launch of the context goes to. */
+void* mbg_stream(const mbg_ctx* ctx);
+
+/* Per-kernel timing with CUDA events recorded around each launch on the
+ * context's stream (off by default; enabling it resets the totals).
+ * mbg_timing(k) reports kernel class k (0 .. mbg_timing_count()-1): its
+ * name, the number of launches and their summed device time in ms. */
+mbg_status mbg_set_timing(mbg_ctx* ctx, int enable);
+int mbg_timing_count(void);
+mbg_status mbg_timing(mbg_ctx* ctx, int k, const char** name, long long* launches, double* ms);
+
+/* ---- host drop-in driver ----------------------------------------------
+ * The reference's LBM/AmrCore driver (Source/LBM.H:25-319, main.cpp:10-25)
+ * on top of the entry points above: reads an inputs file with the
+ * reference's keys (amr.*, geometry.*, lbm.*, ic_<type>.*,
+ * velocity_bc_<type>.*, eb2.*, tagging.*) plus "key=value" overrides, builds
+ * static grids, EB flags and the initial state, and runs the time loop. */
+typedef struct mbg_lbm mbg_lbm;
+
+/* Parse inputs text (and overrides) and select the IC / velocity-BC
+ * functors.  Replaces LBM::LBM() and read_parameters (Source/LBM.cpp:6-300)
+ * with set_ics / set_bcs (LBM.cpp:1382-1476). */
+mbg_status mbg_lbm_create(const char* inputs_text, int n_overrides, const char* const* overrides, mbg_lbm** out);
+
+/* Grids, flags, initial state and the initial average_down.  Replaces
+ * LBM::init_data (Source/LBM.cpp:155-194). */
+mbg_status mbg_lbm_init(mbg_lbm* h);
+
+/* nsteps coarse steps (nsteps <= 0: until max_step / stop_time), with
+ * forces and plotfiles at their intervals.  Replaces LBM::evolve
+ * (Source/LBM.cpp:398-448). */
+mbg_status mbg_lbm_evolve(mbg_lbm* h, int nsteps);
+
+/* Host-only part of init_data: grids (level 0 chopped by
+ * amr.max_grid_size, finer levels from tagging.*) and is_fluid flags.
+ * Replaces AmrCore::InitFromScratch's grid creation with
+ * initialize_is_fluid (Source/LBM.cpp:165, 1213-1262). */
+mbg_status mbg_lbm_prepare(mbg_lbm* h);
+
+/* Initial f and g of level lev on the host (valid cells; layout of
+ * mbg_set_state), from the selected IC functor and fill_f_inside_eb.
+ * Replaces Initializer::initialize (Source/IC.H:460-525) and
+ * LBM::fill_f_inside_eb (Source/LBM.cpp:1278-1298). */
+mbg_status mbg_lbm_initial_state(mbg_lbm* h, int lev, double* f, double* g);
+
+/* The level-step context the driver runs on (owned by the driver). */
+mbg_ctx* mbg_lbm_context(mbg_lbm* h);
+
+/* Grids and is_fluid flags the driver built (layout of mbg_define_level). */
+int mbg_lbm_num_levels(const mbg_lbm* h);
+mbg_status mbg_lbm_level_boxes(const mbg_lbm* h, int lev, int* lohi, int cap, int* nbox);
+mbg_status mbg_lbm_level_flags(const mbg_lbm* h, int lev, uint8_t* out, long long cap, long long* n);
+
+/* AMReX plotfile of the current state.  Replaces LBM::write_plot_file
+ * (Source/LBM.cpp:1677-1690). */
+mbg_status mbg_lbm_write_plotfile(mbg_lbm* h, const char* name);
+
+const char* mbg_lbm_last_error(const mbg_lbm* h);
+void mbg_lbm_destroy(mbg_lbm* h);
+
 #ifdef __cplusplus
 }
 #endif

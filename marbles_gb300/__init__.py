@@ -23,6 +23,10 @@ EXPORTS = [
     "mbg_create", "mbg_destroy", "mbg_last_error", "mbg_define_level", "mbg_level_cells",
     "mbg_set_state", "mbg_get_state", "mbg_get_macro", "mbg_step", "mbg_advance_level",
     "mbg_fillpatch", "mbg_average_down", "mbg_eb_forces", "mbg_synchronize", "mbg_launch_count",
+    "mbg_stream", "mbg_set_timing", "mbg_timing_count", "mbg_timing",
+    "mbg_lbm_create", "mbg_lbm_prepare", "mbg_lbm_initial_state", "mbg_lbm_init", "mbg_lbm_evolve", "mbg_lbm_context", "mbg_lbm_num_levels",
+    "mbg_lbm_level_boxes", "mbg_lbm_level_flags", "mbg_lbm_write_plotfile", "mbg_lbm_last_error",
+    "mbg_lbm_destroy",
 ]
 
 
@@ -79,6 +83,28 @@ def lib():
         L.mbg_synchronize.argtypes = [vp]
         L.mbg_launch_count.argtypes = [vp]
         L.mbg_launch_count.restype = C.c_longlong
+        L.mbg_stream.argtypes = [vp]
+        L.mbg_stream.restype = vp
+        L.mbg_set_timing.argtypes = [vp, C.c_int]
+        L.mbg_timing_count.argtypes = []
+        L.mbg_timing.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_longlong),
+                                 C.POINTER(C.c_double)]
+        L.mbg_lbm_create.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(vp)]
+        L.mbg_lbm_init.argtypes = [vp]
+        L.mbg_lbm_prepare.argtypes = [vp]
+        L.mbg_lbm_initial_state.argtypes = [vp, C.c_int, dp, dp]
+        L.mbg_lbm_evolve.argtypes = [vp, C.c_int]
+        L.mbg_lbm_context.argtypes = [vp]
+        L.mbg_lbm_context.restype = vp
+        L.mbg_lbm_num_levels.argtypes = [vp]
+        L.mbg_lbm_level_boxes.argtypes = [vp, C.c_int, ip, C.c_int, ip]
+        L.mbg_lbm_level_flags.argtypes = [vp, C.c_int, C.POINTER(C.c_uint8), C.c_longlong,
+                                          C.POINTER(C.c_longlong)]
+        L.mbg_lbm_write_plotfile.argtypes = [vp, C.c_char_p]
+        L.mbg_lbm_last_error.argtypes = [vp]
+        L.mbg_lbm_last_error.restype = C.c_char_p
+        L.mbg_lbm_destroy.argtypes = [vp]
+        L.mbg_lbm_destroy.restype = None
         _lib = L
     return _lib
 
@@ -186,9 +212,101 @@ class Context:
     def launch_count(self):
         return self.L.mbg_launch_count(self.h)
 
+    def stream(self):
+        return self.L.mbg_stream(self.h)
+
+    def set_timing(self, on):
+        self._check(self.L.mbg_set_timing(self.h, 1 if on else 0), "mbg_set_timing")
+
+    def timing(self):
+        """{kernel class: (launches, total device ms)} since timing was enabled."""
+        out = {}
+        for k in range(self.L.mbg_timing_count()):
+            name, n, ms = C.c_char_p(), C.c_longlong(), C.c_double()
+            self._check(self.L.mbg_timing(self.h, k, C.byref(name), C.byref(n), C.byref(ms)), "mbg_timing")
+            out[name.value.decode()] = (n.value, ms.value)
+        return out
+
     def close(self):
         if getattr(self, "h", None):
             self.L.mbg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LBM:
+    """The host drop-in driver: inputs text with the reference's keys."""
+
+    def __init__(self, inputs_text, overrides=()):
+        self.L = lib()
+        h = C.c_void_p()
+        ov = (C.c_char_p * max(1, len(overrides)))(*[o.encode() for o in overrides])
+        st = self.L.mbg_lbm_create(inputs_text.encode(), len(overrides), ov, C.byref(h))
+        if st != 0:
+            raise MbgError("mbg_lbm_create: %s: %s" % (STATUS.get(st, st), self.L.mbg_lbm_last_error(None).decode()))
+        self.h = h
+        self.ctx = None
+
+    def _check(self, st, what):
+        if st != 0:
+            raise MbgError("%s: %s: %s" % (what, STATUS.get(st, st), self.L.mbg_lbm_last_error(self.h).decode()))
+
+    def init(self):
+        self._check(self.L.mbg_lbm_init(self.h), "mbg_lbm_init")
+        ctx = Context.__new__(Context)
+        ctx.L = self.L
+        ctx.h = C.c_void_p(self.L.mbg_lbm_context(self.h))
+        ctx.p = None
+        ctx.boxes = [self.boxes(l) for l in range(self.num_levels())]
+        ctx.close = lambda: None        # owned by the driver
+        self.ctx = ctx
+        return ctx
+
+    def evolve(self, nsteps):
+        self._check(self.L.mbg_lbm_evolve(self.h, nsteps), "mbg_lbm_evolve")
+
+    def prepare(self):
+        """Grids and flags on the host (no GPU work)."""
+        self._check(self.L.mbg_lbm_prepare(self.h), "mbg_lbm_prepare")
+
+    def initial_state(self, lev):
+        b = self.boxes(lev)
+        n = int(np.prod(b[:, 3:] - b[:, :3] + 1, axis=1).sum())
+        f = np.empty(n * NQ)
+        g = np.empty(n * NQ)
+        self._check(self.L.mbg_lbm_initial_state(self.h, lev, _dp(f), _dp(g)), "mbg_lbm_initial_state")
+        return f, g
+
+    def num_levels(self):
+        return self.L.mbg_lbm_num_levels(self.h)
+
+    def boxes(self, lev):
+        n = C.c_int()
+        self._check(self.L.mbg_lbm_level_boxes(self.h, lev, None, 0, C.byref(n)), "mbg_lbm_level_boxes")
+        out = np.zeros(6 * n.value, dtype=np.int32)
+        self._check(self.L.mbg_lbm_level_boxes(self.h, lev, out.ctypes.data_as(C.POINTER(C.c_int)), n.value,
+                                               C.byref(n)), "mbg_lbm_level_boxes")
+        return out.reshape(-1, 6)
+
+    def flags(self, lev):
+        n = C.c_longlong()
+        self._check(self.L.mbg_lbm_level_flags(self.h, lev, None, 0, C.byref(n)), "mbg_lbm_level_flags")
+        out = np.zeros(n.value, dtype=np.uint8)
+        self._check(self.L.mbg_lbm_level_flags(self.h, lev, out.ctypes.data_as(C.POINTER(C.c_uint8)), n.value,
+                                               C.byref(n)), "mbg_lbm_level_flags")
+        return out
+
+    def write_plotfile(self, name):
+        self._check(self.L.mbg_lbm_write_plotfile(self.h, name.encode()), "mbg_lbm_write_plotfile")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mbg_lbm_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -14,12 +14,17 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmarbles_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
+# host code: no FMA contraction either (aarch64 g++ contracts by default)
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp",
+          "--expt-relaxed-constexpr"] + ARCH
 UNITS = {
     "mbg_fp64.cu": ["-fmad=false"],
     "mbg_lowp.cu": [],
     "mbg_capi.cu": [],
+    "lbm_driver.cu": [],
+    "lbm_capi.cu": [],
 }
+EXE = os.path.join(HERE, "marbles_gb300_run")
 
 
 def nvcc():
@@ -54,10 +59,16 @@ def build(force=False, verbose=True):
         return LIB
     with ThreadPoolExecutor(max_workers=len(units)) as ex:
         objs = list(ex.map(lambda kv: _compile(*kv), units.items()))
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-Xcompiler", "-fopenmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    main = os.path.join(CSRC, "marbles_main.cpp")
+    cmd = [nvcc(), "-O2", "-std=c++17", main, "-o", EXE, "-L" + HERE, "-lmarbles_gpu",
+           "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("executable link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     if verbose:
         print("built", LIB, file=sys.stderr)
     return LIB

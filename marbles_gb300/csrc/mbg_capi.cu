@@ -69,8 +69,18 @@ struct Level {
 
 }  // namespace
 
+// kernel classes timed by mbg_set_timing
+enum { TK_MOMENTS = 0, TK_COLLIDE, TK_GHOST_STREAM, TK_GHOST_MOMENTS, TK_EXPLODE, TK_COALESCE, TK_FUSED, TK_OTHER, TK_N };
+static const char* TK_NAMES[TK_N] = {"k_moments", "k_collide", "k_ghost_stream", "k_ghost_moments",
+                                     "k_explode", "k_coalesce", "k_lowp_fused", "other"};
+
 struct mbg_ctx {
     mbg_params p;
+    bool timing = false;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
+    std::vector<cudaEvent_t> event_pool;
+    long long tk_count[TK_N] = {};
+    double tk_ms[TK_N] = {};
     cudaStream_t s = nullptr;
     bool own_stream = false;
     std::vector<Level> lv;
@@ -99,6 +109,48 @@ static mbg_status fail(mbg_ctx* ctx, mbg_status st, const std::string& m)
 {
     ctx->err = m;
     return st;
+}
+
+static cudaEvent_t take_event(mbg_ctx* ctx)
+{
+    if (!ctx->event_pool.empty()) {
+        cudaEvent_t e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// records an event pair around the launches issued by `launch`
+template <class F>
+static void timed(mbg_ctx* ctx, int k, F&& launch)
+{
+    if (!ctx->timing) {
+        launch();
+        return;
+    }
+    cudaEvent_t a = take_event(ctx), b = take_event(ctx);
+    cudaEventRecord(a, ctx->s);
+    launch();
+    cudaEventRecord(b, ctx->s);
+    ctx->events.push_back({k, {a, b}});
+}
+
+static void drain_events(mbg_ctx* ctx)
+{
+    if (ctx->events.empty()) return;
+    cudaStreamSynchronize(ctx->s);
+    for (auto& e : ctx->events) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e.second.first, e.second.second);
+        ctx->tk_count[e.first] += 1;
+        ctx->tk_ms[e.first] += ms;
+        ctx->event_pool.push_back(e.second.first);
+        ctx->event_pool.push_back(e.second.second);
+    }
+    ctx->events.clear();
 }
 
 template <class T>
@@ -267,6 +319,8 @@ void mbg_destroy(mbg_ctx* ctx)
 {
     if (!ctx) return;
     if (ctx->s) cudaStreamSynchronize(ctx->s);
+    drain_events(ctx);
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     for (void* q : ctx->allocs) cudaFree(q);
     if (ctx->own_stream && ctx->s) cudaStreamDestroy(ctx->s);
     delete ctx;
@@ -462,54 +516,56 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
             mbg_status st = dalloc(ctx, dst, cl.size());
             if (st != MBG_OK) return st;
             if (!cl.empty())
-                MBG_CUDA(cudaMemcpy(*dst, cl.data(), cl.size() * sizeof(CoalesceCell), cudaMemcpyHostToDevice));
+                MBG_CUDA(cudaMemcpyAsync(*dst, cl.data(), cl.size() * sizeof(CoalesceCell), cudaMemcpyHostToDevice, ctx->s));
             *cnt = (long long)cl.size();
         }
         // re-upload the coarse flags with the coalescence bits
-        MBG_CUDA(cudaMemcpy(C.d_flags, C.hflags.data(), C.hflags.size(), cudaMemcpyHostToDevice));
+        MBG_CUDA(cudaMemcpyAsync(C.d_flags, C.hflags.data(), C.hflags.size(), cudaMemcpyHostToDevice, ctx->s));
     }
     // device allocations
     mbg_status st;
     if ((st = dalloc(ctx, &L.d_box, nbox)) != MBG_OK) return st;
-    MBG_CUDA(cudaMemcpy(L.d_box, L.hbox.data(), nbox * sizeof(DevBox), cudaMemcpyHostToDevice));
+    MBG_CUDA(cudaMemcpyAsync(L.d_box, L.hbox.data(), nbox * sizeof(DevBox), cudaMemcpyHostToDevice, ctx->s));
     if ((st = dalloc(ctx, &L.d_omap, L.omap.size())) != MBG_OK) return st;
-    MBG_CUDA(cudaMemcpy(L.d_omap, L.omap.data(), L.omap.size() * sizeof(int), cudaMemcpyHostToDevice));
+    MBG_CUDA(cudaMemcpyAsync(L.d_omap, L.omap.data(), L.omap.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     if ((st = dalloc(ctx, &L.d_flags, L.hflags.size())) != MBG_OK) return st;
-    MBG_CUDA(cudaMemcpy(L.d_flags, L.hflags.data(), L.hflags.size(), cudaMemcpyHostToDevice));
+    MBG_CUDA(cudaMemcpyAsync(L.d_flags, L.hflags.data(), L.hflags.size(), cudaMemcpyHostToDevice, ctx->s));
     std::vector<Tile> tiles;
     for (int n = 0; n < nbox; ++n)
         for (long long s = 0; s < L.boxes[n].vol(); s += TILE_CELLS) tiles.push_back(Tile{n, (int)s});
     L.ntiles = (int)tiles.size();
     if ((st = dalloc(ctx, &L.d_tiles, tiles.size())) != MBG_OK) return st;
-    MBG_CUDA(cudaMemcpy(L.d_tiles, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice));
+    MBG_CUDA(cudaMemcpyAsync(L.d_tiles, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, ctx->s));
     L.nghost = (long long)ghosts.size();
     L.nghost1 = (long long)ghosts1.size();
     if ((st = dalloc(ctx, &L.d_ghost, ghosts.size())) != MBG_OK) return st;
     if ((st = dalloc(ctx, &L.d_ghost1, ghosts1.size())) != MBG_OK) return st;
     if (!ghosts.empty())
-        MBG_CUDA(cudaMemcpy(L.d_ghost, ghosts.data(), ghosts.size() * sizeof(GhostCell), cudaMemcpyHostToDevice));
+        MBG_CUDA(cudaMemcpyAsync(L.d_ghost, ghosts.data(), ghosts.size() * sizeof(GhostCell), cudaMemcpyHostToDevice, ctx->s));
     if (!ghosts1.empty())
-        MBG_CUDA(cudaMemcpy(L.d_ghost1, ghosts1.data(), ghosts1.size() * sizeof(GhostCell), cudaMemcpyHostToDevice));
+        MBG_CUDA(cudaMemcpyAsync(L.d_ghost1, ghosts1.data(), ghosts1.size() * sizeof(GhostCell), cudaMemcpyHostToDevice, ctx->s));
     if (p.precision == MBG_FP64) {
         for (int b = 0; b < 2; ++b) {
             if ((st = dalloc(ctx, &L.f[b], (size_t)L.N * NQ)) != MBG_OK) return st;
             if ((st = dalloc(ctx, &L.g[b], (size_t)L.N * NQ)) != MBG_OK) return st;
-            MBG_CUDA(cudaMemset(L.f[b], 0, (size_t)L.N * NQ * sizeof(double)));
-            MBG_CUDA(cudaMemset(L.g[b], 0, (size_t)L.N * NQ * sizeof(double)));
+            MBG_CUDA(cudaMemsetAsync(L.f[b], 0, (size_t)L.N * NQ * sizeof(double), ctx->s));
+            MBG_CUDA(cudaMemsetAsync(L.g[b], 0, (size_t)L.N * NQ * sizeof(double), ctx->s));
             if (L.NG > 0) {
                 if ((st = dalloc(ctx, &L.fg[b], (size_t)L.NG * NQ)) != MBG_OK) return st;
                 if ((st = dalloc(ctx, &L.gg[b], (size_t)L.NG * NQ)) != MBG_OK) return st;
-                MBG_CUDA(cudaMemset(L.fg[b], 0, (size_t)L.NG * NQ * sizeof(double)));
-                MBG_CUDA(cudaMemset(L.gg[b], 0, (size_t)L.NG * NQ * sizeof(double)));
+                MBG_CUDA(cudaMemsetAsync(L.fg[b], 0, (size_t)L.NG * NQ * sizeof(double), ctx->s));
+                MBG_CUDA(cudaMemsetAsync(L.gg[b], 0, (size_t)L.NG * NQ * sizeof(double), ctx->s));
             }
         }
         if ((st = dalloc(ctx, &L.md, (size_t)L.N * MD_NCOMP)) != MBG_OK) return st;
-        MBG_CUDA(cudaMemset(L.md, 0, (size_t)L.N * MD_NCOMP * sizeof(double)));
+        MBG_CUDA(cudaMemsetAsync(L.md, 0, (size_t)L.N * MD_NCOMP * sizeof(double), ctx->s));
         if (L.NG > 0) {
             if ((st = dalloc(ctx, &L.gqc, (size_t)L.NG * 3)) != MBG_OK) return st;
-            MBG_CUDA(cudaMemset(L.gqc, 0, (size_t)L.NG * 3 * sizeof(double)));
+            MBG_CUDA(cudaMemsetAsync(L.gqc, 0, (size_t)L.NG * 3 * sizeof(double), ctx->s));
         }
     }
+    // the host staging vectors above must outlive their copies
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
     ctx->lv.push_back(std::move(L));
     Level& LL = ctx->lv.back();
     refresh_plan(ctx, LL);
@@ -604,9 +660,10 @@ static mbg_status explode(mbg_ctx* ctx, int lev)
     Level& F = ctx->lv[lev];
     Level& C = ctx->lv[lev - 1];
     if (ctx->p.precision != MBG_FP64) {
-        lowp_explode(F.lowp, F.plan, C.lowp, C.plan, ctx->s);
+        timed(ctx, TK_EXPLODE, [&] { lowp_explode(F.lowp, F.plan, C.lowp, C.plan, ctx->s); });
     } else {
-        launch_explode(F.plan, C.plan, C.f[C.cur], C.g[C.cur], F.fg[F.cur], F.gg[F.cur], ctx->s);
+        timed(ctx, TK_EXPLODE,
+              [&] { launch_explode(F.plan, C.plan, C.f[C.cur], C.g[C.cur], F.fg[F.cur], F.gg[F.cur], ctx->s); });
     }
     ctx->launches++;
     MBG_CUDA(cudaGetLastError());
@@ -620,8 +677,11 @@ static mbg_status advance(mbg_ctx* ctx, int lev)
     if (ctx->p.precision != MBG_FP64) {
         const LowpLevel* fine = has_finer ? &ctx->lv[lev + 1].lowp : nullptr;
         const LevelPlan* fplan = has_finer ? &ctx->lv[lev + 1].plan : nullptr;
-        int nl = lowp_advance(ctx->p, ctx->bc, L.lowp, L.plan, L.dt, L.idx, has_finer ? L.d_coal1 : nullptr,
+        int nl = 0;
+        timed(ctx, TK_FUSED, [&] {
+            nl = lowp_advance(ctx->p, ctx->bc, L.lowp, L.plan, L.dt, L.idx, has_finer ? L.d_coal1 : nullptr,
                               has_finer ? L.ncoal1 : 0, fine, fplan, ctx->s);
+        });
         ctx->launches += nl;
         MBG_CUDA(cudaGetLastError());
         return MBG_OK;
@@ -630,17 +690,28 @@ static mbg_status advance(mbg_ctx* ctx, int lev)
     const int A = L.cur, Bf = 1 - L.cur;
     if (has_finer) {
         Level& F = ctx->lv[lev + 1];
-        launch_coalesce(L.plan, F.plan, ctx->bc, ph, L.d_coal1, L.ncoal1, F.f[F.cur], F.g[F.cur], F.fg[F.cur],
-                        F.gg[F.cur], L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], 0, ctx->s);
+        timed(ctx, TK_COALESCE, [&] {
+            launch_coalesce(L.plan, F.plan, ctx->bc, ph, L.d_coal1, L.ncoal1, F.f[F.cur], F.g[F.cur], F.fg[F.cur],
+                            F.gg[F.cur], L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], 0, ctx->s);
+        });
         ctx->launches++;
     }
     if (L.NG > 0) {
-        launch_ghost_stream(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.fg[Bf], L.gg[Bf], ctx->s);
-        launch_ghost_moments(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.gqc, ctx->s);
+        timed(ctx, TK_GHOST_STREAM, [&] {
+            launch_ghost_stream(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.fg[Bf], L.gg[Bf], ctx->s);
+        });
+        timed(ctx, TK_GHOST_MOMENTS, [&] {
+            launch_ghost_moments(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.gqc, ctx->s);
+        });
         ctx->launches += 2;
     }
-    launch_moments(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], L.md, ctx->s);
-    launch_collide(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], L.md, L.gqc, ctx->s);
+    timed(ctx, TK_MOMENTS, [&] {
+        launch_moments(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], L.md, ctx->s);
+    });
+    timed(ctx, TK_COLLIDE, [&] {
+        launch_collide(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], L.md, L.gqc,
+                       ctx->s);
+    });
     ctx->launches += 2;
     MBG_CUDA(cudaGetLastError());
     L.cur = Bf;
@@ -720,6 +791,29 @@ mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3])
     MBG_CUDA(cudaGetLastError());
     MBG_CUDA(cudaMemcpyAsync(out, ctx->d_red, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
     MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+void* mbg_stream(const mbg_ctx* ctx) { return ctx ? (void*)ctx->s : nullptr; }
+
+mbg_status mbg_set_timing(mbg_ctx* ctx, int enable)
+{
+    if (!ctx) return MBG_EINVAL;
+    drain_events(ctx);
+    ctx->timing = enable != 0;
+    for (int k = 0; k < TK_N; ++k) { ctx->tk_count[k] = 0; ctx->tk_ms[k] = 0.0; }
+    return MBG_OK;
+}
+
+int mbg_timing_count(void) { return TK_N; }
+
+mbg_status mbg_timing(mbg_ctx* ctx, int k, const char** name, long long* launches, double* ms)
+{
+    if (!ctx || k < 0 || k >= TK_N) return MBG_EINVAL;
+    drain_events(ctx);
+    if (name) *name = TK_NAMES[k];
+    if (launches) *launches = ctx->tk_count[k];
+    if (ms) *ms = ctx->tk_ms[k];
     return MBG_OK;
 }
 
