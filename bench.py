@@ -114,11 +114,22 @@ def run_form(form, steps, warmup, device_index):
     import torch
     import marbles_gb300 as M
 
+    import ctypes as C
     d = M.LBM(inputs_text(), ["lbm.precision=" + form])
     ctx = d.init()
     nlev = d.num_levels()
     cups = cell_updates_per_step(ctx, nlev)
     stream = torch.cuda.ExternalStream(ctx.stream())
+    # the initial state in pinned host buffers (input of the end-to-end leg)
+    dp = C.POINTER(C.c_double)
+    lib = M.lib()
+    host = []
+    for lev in range(nlev):
+        n = ctx.ncells(lev) * M.NQ
+        f = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        g = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+        host.append((f, g))
     for _ in range(warmup):
         ctx.step(1)
     ctx.synchronize()
@@ -141,19 +152,8 @@ def run_form(form, steps, warmup, device_index):
            "kernels": {k: {"launches": n, "ms": t} for k, (n, t) in timing.items() if n},
            "clocks": clk.summary()}
     # end to end through the C ABI with pinned host buffers: upload of the
-    # state, K steps each followed by the EB-force read-back (the reference
-    # computes it every step), download of the state
-    host = []
-    for lev in range(nlev):
-        n = ctx.ncells(lev) * M.NQ
-        f = torch.empty(n, dtype=torch.float64, pin_memory=True)
-        g = torch.empty(n, dtype=torch.float64, pin_memory=True)
-        host.append((f, g))
-    import ctypes as C
-    dp = C.POINTER(C.c_double)
-    lib = M.lib()
-    for lev, (f, g) in enumerate(host):
-        ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+    # initial state, K steps each followed by the EB-force read-back (the
+    # reference computes it every step), download of the state
     forces = torch.zeros(3, dtype=torch.float64, pin_memory=True)
     ctx.synchronize()
     t0 = time.perf_counter()

@@ -36,7 +36,8 @@ __device__ __forceinline__ double pull(const LV& L, const BCParams& P, const Dev
     const uint8_t sf = flag_at(L, B, sx, sy, sz);
     if (!(sf & FL_FLUID)) return fab_value(L, B, x, y, z, oq, v, vg);
     int gp[3] = {B.lo[0] + sx, B.lo[1] + sy, B.lo[2] + sz};
-    if (outside_nonperiodic(L, gp)) return bc_value<q, double, double>(L, P, B, sx, sy, sz, is_g, v, vg, lat);
+    if (outside_nonperiodic(L, gp))
+        return bc_value<q, double, double>(L, P, B, sx, sy, sz, is_g, v, vg, lat, [](double r, int) { return r; });
     return fab_value(L, B, sx, sy, sz, q, v, vg);
 }
 
@@ -382,7 +383,8 @@ __global__ void k_macro_local(LV L, Phys64 ph, const Tile* tiles, const double* 
 }
 
 // ---- EB momentum-exchange force (Source/LBM.cpp:994-1044) -------------------
-// per-cell sums in FP64, reduced with warp shuffles and one atomic per warp
+// per-cell sums in FP64; only eb_boundary cells contribute (a thin shell), so
+// each such cell adds its three components with FP64 atomics
 __global__ void k_eb_forces(LV L, const Tile* tiles, const double* f, const double* fg, double* out3)
 {
     int b, x, y, z;
@@ -406,11 +408,8 @@ __global__ void k_eb_forces(LV L, const Tile* tiles, const double* f, const doub
             });
         }
     }
-    for (int d = 0; d < 3; ++d) {
-        double v = fs[d];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if ((threadIdx.x & 31) == 0 && v != 0.0) atomicAdd(&out3[d], v);
-    }
+    for (int d = 0; d < 3; ++d)
+        if (fs[d] != 0.0) atomicAdd(&out3[d], fs[d]);
 }
 
 // ---- launchers -----------------------------------------------------------

@@ -125,6 +125,12 @@ __device__ __forceinline__ bool outside_nonperiodic(const LevelView<S>& L, const
     return false;
 }
 
+// raw storage value of the -1 sentinel (16-bit forms reserve a NaN code)
+template <class S>
+__device__ __forceinline__ S sentinel_raw() { return (S)-1.0; }
+template <>
+__device__ __forceinline__ uint16_t sentinel_raw<uint16_t>() { return (uint16_t)0xFFFFu; }
+
 // Value of a component array at box-local position (x,y,z) of box B's fab
 // (valid, covered ghost or uncovered ghost).  The position must not lie
 // outside a non-periodic side of the domain.
@@ -140,7 +146,7 @@ __device__ __forceinline__ S fab_value(const LevelView<S>& L, const DevBox& B, i
         const DevBox& O = L.box[o];
         return v[q * L.N + O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2])];
     }
-    if (B.goff < 0 || vg == nullptr) return (S)-1.0;  // no storage there (plans exclude this case)
+    if (B.goff < 0 || vg == nullptr) return sentinel_raw<S>();  // no storage there (plans exclude this case)
     return vg[q * L.NG + B.goff + fab_lin(B, x, y, z)];
 }
 
@@ -179,9 +185,9 @@ __device__ inline void vel_bc_state(const BCParams& P, const int dhi[3], const i
 // non-periodic side that s lies outside of decides.  Outflow reads the
 // next cell inward, which may itself be a ghost on another side (edges and
 // corners): the loop then continues from that cell.
-template <int q, class S, class R>
+template <int q, class S, class R, class Dec>
 __device__ R bc_value(const LevelView<S>& L, const BCParams& P, const DevBox& B, int sx, int sy, int sz,
-                      bool is_g, const S* v, const S* vg, const Lattice<R>& lat)
+                      bool is_g, const S* v, const S* vg, const Lattice<double>& lat, const Dec& dec)
 {
     constexpr int bq = opp(q), mx = mirror(q, 0), my = mirror(q, 1), mz = mirror(q, 2);
     constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
@@ -201,28 +207,21 @@ __device__ R bc_value(const LevelView<S>& L, const BCParams& P, const DevBox& B,
         const int tx = s[0] + ex, ty = s[1] + ey, tz = s[2] + ez;
         switch (bc) {
         case 1:  // no-slip: data(iv + ev, bounce(q))
-            return (R)fab_value(L, B, tx, ty, tz, bq, v, vg);
-        case 6: return (R)fab_value(L, B, tx, ty, tz, mx, v, vg);
-        case 7: return (R)fab_value(L, B, tx, ty, tz, my, v, vg);
-        case 8: return (R)fab_value(L, B, tx, ty, tz, mz, v, vg);
+            return dec(fab_value(L, B, tx, ty, tz, bq, v, vg), bq);
+        case 6: return dec(fab_value(L, B, tx, ty, tz, mx, v, vg), mx);
+        case 7: return dec(fab_value(L, B, tx, ty, tz, my, v, vg), my);
+        case 8: return dec(fab_value(L, B, tx, ty, tz, mz, v, vg), mz);
         case 2: {  // velocity
             int gp[3] = {B.lo[0] + s[0], B.lo[1] + s[1], B.lo[2] + s[2]};
             double vel[3] = {0.0, 0.0, 0.0}, Rg = 1.0, temp = 1.0 / 3.0, gamma = 5.0 / 3.0, rho = 0.0;
             vel_bc_state(P, L.dhi, gp, rho, vel, Rg, temp, gamma);
-            if (is_g) {
-                Lattice<double> ld;
-#pragma unroll
-                for (int k = 0; k < NQ; ++k) ld.w[k] = (double)lat.w[k];
-                ld.theta0 = (double)lat.theta0; ld.one_bystheta0 = (double)lat.one_bystheta0;
-                ld.cth[0] = (double)lat.cth[0]; ld.cth[1] = (double)lat.cth[1];
-                return (R)eq_g_plain<double>(q, rho, vel, Rg, temp, gamma, ld);
-            }
+            if (is_g) return (R)eq_g_plain<double>(q, rho, vel, Rg, temp, gamma, lat);
             return (R)eq_f_plain<double>(q, rho, vel, Rg * temp);
         }
         case 5: {  // outflow: data(iv + ndir e_idir, q)
             s[idir] += ndir;
             int gp[3] = {B.lo[0] + s[0], B.lo[1] + s[1], B.lo[2] + s[2]};
-            if (!outside_nonperiodic(L, gp)) return (R)fab_value(L, B, s[0], s[1], s[2], q, v, vg);
+            if (!outside_nonperiodic(L, gp)) return dec(fab_value(L, B, s[0], s[1], s[2], q, v, vg), q);
             continue;
         }
         default:

@@ -1372,6 +1372,12 @@ int orc_fillpatch(void* h, int lev)
     return 0;
 }
 
+int orc_average_down(void* h, int crse_lev, int ng)
+{
+    static_cast<Sim*>(h)->average_down_to(crse_lev, ng);
+    return 0;
+}
+
 long long orc_level_cells(void* h, int lev)
 {
     auto* s = static_cast<Sim*>(h);

@@ -77,6 +77,7 @@ def lib():
         L.orc_step.argtypes = [vp, C.c_int]
         L.orc_advance_level.argtypes = [vp, C.c_int]
         L.orc_fillpatch.argtypes = [vp, C.c_int]
+        L.orc_average_down.argtypes = [vp, C.c_int, C.c_int]
         L.orc_level_cells.restype = C.c_longlong
         L.orc_level_cells.argtypes = [vp, C.c_int]
         dp = C.POINTER(C.c_double)
@@ -178,6 +179,9 @@ class Oracle:
 
     def step(self, n=1):
         self.L.orc_step(self.h, n)
+
+    def average_down(self, crse_lev, ng):
+        self.L.orc_average_down(self.h, crse_lev, ng)
 
     def ncells(self, lev):
         return self.L.orc_level_cells(self.h, lev)

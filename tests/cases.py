@@ -65,7 +65,7 @@ def taylor_green(n=64, mgs=32, nu=0.005, v0=0.05):
     return p, [chop([0, 0, 0], [n - 1] * 3, mgs)]
 
 
-def gaussian_pulse(nc=128, fine_lo=32, fine_hi=95, mgs=32, nu=0.01, amp=0.01, width=8.0):
+def gaussian_pulse(nc=128, fine_lo=32, fine_hi=95, mgs=32, nu=0.01, amp=0.01, width=8.0, t0=1.0 / 3.0):
     """Two-level pulse: coarse nc^3 periodic, fine level (ratio 2) over the
     coarse cells [fine_lo, fine_hi]^3; rho = 1 + amp exp(-r^2 / (2 width^2))."""
     p = O.default_params()
@@ -81,14 +81,15 @@ def gaussian_pulse(nc=128, fine_lo=32, fine_hi=95, mgs=32, nu=0.01, amp=0.01, wi
     p.ic_pulse_amplitude = amp
     p.ic_pulse_width = width
     p.ic_pulse_center[:] = [nc / 2.0] * 3
-    p.ic_initial_temperature = 1.0 / 3.0
+    p.ic_initial_temperature = t0
+    p.initial_temperature = t0
     lev0 = chop([0, 0, 0], [nc - 1] * 3, mgs)
     lev1 = chop([2 * fine_lo] * 3, [2 * fine_hi + 1] * 3, mgs)
     return p, [lev0, lev1]
 
 
 def sphere_channel(nx=64, ny=32, nz=32, radius=6.0, center=(20.0, 16.0, 16.0), mgs=16, nu=0.016,
-                   mach=0.0670820, levels=1, bc_lo=(2, 0, 0), bc_hi=(5, 0, 0)):
+                   mach=0.0670820, levels=1, bc_lo=(2, 0, 0), bc_hi=(5, 0, 0), t0=1.0 / 3.0):
     """Flow past a sphere: velocity inflow at x-lo, outflow at x-hi,
     periodic in y and z, constant velocity BC with u = Mach * c_s."""
     p = O.default_params()
@@ -104,6 +105,9 @@ def sphere_channel(nx=64, ny=32, nz=32, radius=6.0, center=(20.0, 16.0, 16.0), m
     p.velbc_type = O.VBC_TYPES["constant"]
     p.vbc_dir = 0
     p.vbc_mach_ref = mach
+    p.vbc_initial_temperature = t0
+    p.ic_initial_temperature = t0
+    p.initial_temperature = t0
     p.ic_type = O.IC_TYPES["constant"]
     p.ic_density = 1.0
     p.ic_mach[:] = [mach, 0.0, 0.0]

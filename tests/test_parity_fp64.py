@@ -5,6 +5,12 @@ after the same number of coarse steps the populations f, g and the macro
 fields rho, u, T must agree to 1e-12 relative (the FP64 form compiles with
 -fmad=false and keeps the reference's operand order, so they are normally
 bit-identical).
+
+The reference's scheme is linearly unstable near RT = 1/3 at low viscosity
+(a perturbed rest state grows about 1.9x per step at nu = 0.01), so
+multi-step cases use the reference's own Taylor-Green viscosity (0.1733) or
+RT <= 0.1; the literal Taylor-Green parameters (nu = 0.005) are compared over
+the steps before the divergence sets in.
 """
 import numpy as np
 import pytest
@@ -56,12 +62,24 @@ def _compare(ctx, o, nlev, rtol=RTOL):
 
 
 def test_taylor_green_64_200_steps():
-    """Taylor-Green 64^3 periodic, 8 boxes of 32^3, 200 steps."""
-    p, levels = cases.taylor_green(64, 32)
+    """Taylor-Green 64^3 on [0, 2 pi)^3, 8 boxes of 32^3, u0 = 0.05, at the
+    viscosity of the reference's own Taylor-Green case, 200 steps."""
+    p, levels = cases.taylor_green(64, 32, nu=0.1733333333333333)
     o = cases.run_oracle(p, levels, 0)
     ctx = _gpu_from_oracle(o, p, levels)
     ctx.step(200)
     o.step(200)
+    _compare(ctx, o, 1)
+
+
+def test_taylor_green_64_literal_parameters_before_divergence():
+    """nu = 0.005 (the workload's literal value): bit-level agreement over the
+    30 steps before the reference scheme's instability grows."""
+    p, levels = cases.taylor_green(64, 32)
+    o = cases.run_oracle(p, levels, 0)
+    ctx = _gpu_from_oracle(o, p, levels)
+    ctx.step(30)
+    o.step(30)
     _compare(ctx, o, 1)
 
 
@@ -87,11 +105,11 @@ def test_single_box_periodic_self_wrap():
 
 def test_sphere_inflow_outflow_single_level():
     """EB sphere, velocity inflow x-lo, outflow x-hi, periodic y/z."""
-    p, levels = cases.sphere_channel(64, 32, 32, radius=6.0, center=(20.0, 16.0, 16.0), mgs=16)
+    p, levels = cases.sphere_channel(64, 32, 32, radius=6.0, center=(20.0, 16.0, 16.0), mgs=16, t0=0.03)
     o = cases.run_oracle(p, levels, 0)
     ctx = _gpu_from_oracle(o, p, levels)
-    ctx.step(20)
-    o.step(20)
+    ctx.step(40)
+    o.step(40)
     _compare(ctx, o, 1)
 
 
@@ -100,7 +118,7 @@ def test_sphere_inflow_outflow_single_level():
 def test_wall_boundaries(bc_lo, bc_hi):
     """No-slip and slip walls, including edges and corners of walls."""
     p, levels = cases.sphere_channel(32, 24, 16, radius=4.0, center=(12.0, 12.0, 8.0), mgs=16,
-                                     bc_lo=bc_lo, bc_hi=bc_hi)
+                                     bc_lo=bc_lo, bc_hi=bc_hi, t0=0.03)
     o = cases.run_oracle(p, levels, 0)
     ctx = _gpu_from_oracle(o, p, levels)
     ctx.step(8)
@@ -110,26 +128,28 @@ def test_wall_boundaries(bc_lo, bc_hi):
 
 def test_gaussian_pulse_two_levels():
     """Explosion, subcycling and coalescence on a small two-level pulse."""
-    p, levels = cases.gaussian_pulse(nc=32, fine_lo=8, fine_hi=23, mgs=16, width=3.0)
+    p, levels = cases.gaussian_pulse(nc=32, fine_lo=8, fine_hi=23, mgs=16, width=3.0, t0=0.1)
     o = cases.run_oracle(p, levels, 0)
     ctx = _gpu_from_oracle(o, p, levels)
-    ctx.step(6)
-    o.step(6)
+    ctx.step(20)
+    o.step(20)
     _compare(ctx, o, 2)
 
 
 def test_sphere_three_levels():
     """Three levels around an EB sphere with inflow/outflow on level 0."""
-    p, levels = cases.sphere_channel(64, 32, 32, radius=5.0, center=(24.0, 16.0, 16.0), mgs=16, levels=3)
+    p, levels = cases.sphere_channel(64, 32, 32, radius=5.0, center=(24.0, 16.0, 16.0), mgs=16, levels=3,
+                                     t0=0.03)
     o = cases.run_oracle(p, levels, 0)
     ctx = _gpu_from_oracle(o, p, levels)
-    ctx.step(3)
-    o.step(3)
+    ctx.step(5)
+    o.step(5)
     _compare(ctx, o, 3)
 
 
 def test_eb_forces_match():
-    p, levels = cases.sphere_channel(48, 24, 24, radius=5.0, center=(16.0, 12.0, 12.0), mgs=16, levels=2)
+    p, levels = cases.sphere_channel(48, 32, 32, radius=5.0, center=(16.0, 16.0, 16.0), mgs=16, levels=2,
+                                     t0=0.03)
     o = cases.run_oracle(p, levels, 0)
     ctx = _gpu_from_oracle(o, p, levels)
     ctx.step(4)
@@ -138,14 +158,34 @@ def test_eb_forces_match():
     assert np.allclose(a, b, rtol=1e-11, atol=1e-13), (a, b)
 
 
-def test_average_down_entry_point():
-    """mbg_average_down (ng = 0 and 1) against the oracle's state after one step."""
-    p, levels = cases.gaussian_pulse(nc=32, fine_lo=8, fine_hi=23, mgs=16, width=3.0)
-    o = cases.run_oracle(p, levels, 1)
+@pytest.mark.parametrize("ng", [0, 1])
+def test_average_down_entry_point(ng):
+    """mbg_average_down against the oracle's average_down_with_ghosts on the
+    state after two steps (fine ghosts then hold streamed values and -1s)."""
+    p, levels = cases.gaussian_pulse(nc=32, fine_lo=8, fine_hi=23, mgs=16, width=3.0, t0=0.1)
+    o = cases.run_oracle(p, levels, 0)
     ctx = _gpu_from_oracle(o, p, levels)
-    # the oracle's state after a step already satisfies the coalescence; the
-    # entry point must leave covered cells equal to the fine averages
-    ctx.average_down(0, 0)
+    ctx.step(2)
+    o.step(2)
+    ctx.average_down(0, ng)
+    o.average_down(0, ng)
     fg, gg = ctx.get_state(0)
     fo, go = o.get_state(0)
     assert _rel(fg, fo) <= RTOL and _rel(gg, go) <= RTOL
+
+
+def test_drop_in_driver_matches_oracle():
+    """The host driver (inputs text -> grids, flags, IC, step) against the
+    oracle on the same inputs: a sphere with two levels at RT = 0.03."""
+    import inputs
+    import marbles_gb300 as M
+    text = inputs.sphere(nx=64, ny=32, nz=32, r=5.0, c=(24.0, 16.0, 16.0), maxlev=1, mgs=16, buf=2)
+    text += "\nic_constant.initial_temperature = 0.03\nvelocity_bc_constant.initial_temperature = 0.03\n"
+    d = M.LBM(text)
+    ctx = d.init()
+    levels = [d.boxes(l) for l in range(d.num_levels())]
+    p, _ = cases.sphere_channel(64, 32, 32, radius=5.0, center=(24.0, 16.0, 16.0), mgs=16, t0=0.03)
+    o = cases.run_oracle(p, levels, 0)
+    d.evolve(6)
+    o.step(6)
+    _compare(ctx, o, len(levels))
