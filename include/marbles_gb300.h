@@ -167,6 +167,29 @@ mbg_status mbg_set_timing(mbg_ctx* ctx, int enable);
 int mbg_timing_count(void);
 mbg_status mbg_timing(mbg_ctx* ctx, int k, const char** name, long long* launches, double* ms);
 
+/* ---- step without device allocation --------------------------------------
+ * No counterpart in the reference.  For callers that cannot let a library
+ * allocate device memory: a host code that has given the GPU to its own
+ * memory arena would risk an out-of-memory failure mid-run, and
+ * cudaMalloc / cudaFree may synchronise the device, which a caller queueing
+ * its time loop asynchronously on its own stream cannot accept.
+ *
+ * One FP64 step (stream, collide, relax: the reference's LBM::advance) of a
+ * single all-fluid box that is periodic in every direction, of
+ * params->n_cell cells (at most MBG_NOALLOC_MAX_CELLS in total), with no
+ * context and no allocation.  f_in, g_in, f_out, g_out are device arrays of
+ * 27 * ncells doubles in [q][k][j][i] order; outputs must not alias inputs.
+ * The scratch between the two passes is a fixed array in the library's
+ * device image (4.5 MiB on every GPU that loads the library, until exit),
+ * shared by all calls: calls whose kernels overlap on the GPU race on it.
+ * The first call on a device looks up that array's address (with the
+ * device current) and should come before any stream capture.  Launches on
+ * cuda_stream (NULL: the legacy default stream); errors are reported by
+ * mbg_last_error(NULL). */
+#define MBG_NOALLOC_MAX_CELLS 32768
+mbg_status mbg_step_box_noalloc(const mbg_params* params, const double* f_in, const double* g_in,
+                                double* f_out, double* g_out, void* cuda_stream);
+
 /* ---- host drop-in driver ----------------------------------------------
  * The reference's LBM/AmrCore driver (Source/LBM.H:25-319, main.cpp:10-25)
  * on top of the entry points above: reads an inputs file with the

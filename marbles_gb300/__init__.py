@@ -23,7 +23,7 @@ EXPORTS = [
     "mbg_create", "mbg_destroy", "mbg_last_error", "mbg_define_level", "mbg_level_cells",
     "mbg_set_state", "mbg_get_state", "mbg_get_macro", "mbg_step", "mbg_advance_level",
     "mbg_fillpatch", "mbg_average_down", "mbg_eb_forces", "mbg_synchronize", "mbg_launch_count",
-    "mbg_stream", "mbg_set_timing", "mbg_timing_count", "mbg_timing",
+    "mbg_stream", "mbg_set_timing", "mbg_timing_count", "mbg_timing", "mbg_step_box_noalloc",
     "mbg_lbm_create", "mbg_lbm_prepare", "mbg_lbm_initial_state", "mbg_lbm_init", "mbg_lbm_evolve", "mbg_lbm_context", "mbg_lbm_num_levels",
     "mbg_lbm_level_boxes", "mbg_lbm_level_flags", "mbg_lbm_write_plotfile", "mbg_lbm_last_error",
     "mbg_lbm_destroy",
@@ -83,6 +83,7 @@ def lib():
         L.mbg_synchronize.argtypes = [vp]
         L.mbg_launch_count.argtypes = [vp]
         L.mbg_launch_count.restype = C.c_longlong
+        L.mbg_step_box_noalloc.argtypes = [C.POINTER(MbgParams), vp, vp, vp, vp, vp]
         L.mbg_stream.argtypes = [vp]
         L.mbg_stream.restype = vp
         L.mbg_set_timing.argtypes = [vp, C.c_int]

@@ -23,6 +23,7 @@ UNITS = {
     "mbg_capi.cu": [],
     "lbm_driver.cu": [],
     "lbm_capi.cu": [],
+    "mbg_noalloc.cu": ["-fmad=false"],
 }
 EXE = os.path.join(HERE, "marbles_gb300_run")
 

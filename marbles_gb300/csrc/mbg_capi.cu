@@ -96,6 +96,8 @@ struct mbg_ctx {
 
 static std::string g_create_err;
 
+void mbg_set_global_error(const std::string& msg) { g_create_err = msg; }
+
 #define MBG_CUDA(call)                                                                   \
     do {                                                                                 \
         cudaError_t e_ = (call);                                                         \
