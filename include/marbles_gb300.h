@@ -78,6 +78,10 @@ typedef struct mbg_params {
     double vbc_initial_temperature;
     double vbc_adiabatic_exponent;
     double vbc_m_bar;
+    /* reference velocity of the shifted 16-bit storage: the rest state above
+     * is taken at (rho_ref, u_ref, T_ref), e.g. the inflow velocity of a
+     * channel flow, so that the stored deviations carry the perturbation only */
+    double u_ref[3];
 } mbg_params;
 
 /* Create a context on the current CUDA device.  cuda_stream may be NULL (the

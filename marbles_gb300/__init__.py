@@ -51,6 +51,7 @@ class MbgParams(C.Structure):
         ("vbc_u_ref", C.c_double), ("vbc_initial_density", C.c_double),
         ("vbc_initial_temperature", C.c_double), ("vbc_adiabatic_exponent", C.c_double),
         ("vbc_m_bar", C.c_double),
+        ("u_ref", C.c_double * 3),
     ]
 
 

@@ -779,6 +779,8 @@ mbg_status LBM::init_data()
     p.precision = cfg_.precision;
     p.rho_ref = ic_.type == 1 ? ic_.rho0 : ic_.density;
     p.t_ref = ic_.type == 1 ? 1.0 / 3.0 : ic_.initial_temperature;
+    if (ic_.type == 0)   // uniform initial flow: the storage shift follows it
+        for (int d = 0; d < 3; ++d) p.u_ref[d] = ic_.mach[d] * ic_.sos;
     p.velbc_type = vbc_.type;
     p.vbc_dir = vbc_.dir; p.vbc_normal_dir = vbc_.normal_dir; p.vbc_tangential_dir = vbc_.tangential_dir;
     p.vbc_u_ref = vbc_.u_ref; p.vbc_initial_density = vbc_.initial_density;

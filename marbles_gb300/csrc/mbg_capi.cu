@@ -323,6 +323,8 @@ void mbg_destroy(mbg_ctx* ctx)
     if (ctx->s) cudaStreamSynchronize(ctx->s);
     drain_events(ctx);
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    for (auto& L : ctx->lv)
+        if (L.lowp.impl) lowp_release(L.lowp);
     for (void* q : ctx->allocs) cudaFree(q);
     if (ctx->own_stream && ctx->s) cudaStreamDestroy(ctx->s);
     delete ctx;
@@ -572,7 +574,7 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     Level& LL = ctx->lv.back();
     refresh_plan(ctx, LL);
     if (p.precision != MBG_FP64) {
-        mbg_status s2 = lowp_define(ctx->p, LL.plan, LL.hbox, LL.N, LL.NG, LL.lowp, ctx->err);
+        mbg_status s2 = lowp_define(ctx->p, LL.plan, LL.hbox, LL.N, LL.NG, LL.dt, LL.idx, LL.lowp, ctx->err);
         if (s2 != MBG_OK) return s2;
     }
     return MBG_OK;
@@ -680,10 +682,11 @@ static mbg_status advance(mbg_ctx* ctx, int lev)
         const LowpLevel* fine = has_finer ? &ctx->lv[lev + 1].lowp : nullptr;
         const LevelPlan* fplan = has_finer ? &ctx->lv[lev + 1].plan : nullptr;
         int nl = 0;
-        timed(ctx, TK_FUSED, [&] {
-            nl = lowp_advance(ctx->p, ctx->bc, L.lowp, L.plan, L.dt, L.idx, has_finer ? L.d_coal1 : nullptr,
-                              has_finer ? L.ncoal1 : 0, fine, fplan, ctx->s);
-        });
+        static const int stage_tk[3] = {TK_COALESCE, TK_GHOST_STREAM, TK_FUSED};
+        nl = lowp_advance(ctx->p, ctx->bc, L.lowp, L.plan, L.dt, L.idx, has_finer ? L.d_coal1 : nullptr,
+                          has_finer ? L.ncoal1 : 0, fine, fplan, ctx->s,
+                          [&](int stage, const std::function<void()>& launch) { timed(ctx, stage_tk[stage], launch); });
+        if (nl < 0) return fail(ctx, MBG_ENOMEM, "16-bit form: allocation of the coalescence buffer failed");
         ctx->launches += nl;
         MBG_CUDA(cudaGetLastError());
         return MBG_OK;

@@ -1,0 +1,129 @@
+// mbg_fp64_amr.cu -- FP64 level-to-level transfers: explosion of the coarse
+// level into a fine level's ghost shell and coalescence of the fine level onto
+// the coarse level.
+#include <cstdio>
+
+#include "mbg_fp64.cuh"
+
+namespace mbg {
+
+// ---- explosion: conservative linear interpolation of the coarse level ------
+// (AMReX cell_cons_interp as called at Source/FillPatchOps.H:124-128: MC
+// slopes, one limiter factor per direction shared by all 27 components)
+__device__ __forceinline__ double crse_at(const LV& C, const int p0[3], int d, int s, int q, const double* v)
+{
+    int p[3] = {p0[0], p0[1], p0[2]};
+    p[d] += s;
+    wrap_pos(C, p);
+    const int o = owner_of(C, p);
+    if (o < 0) return 0.0;  // plans reject fine levels whose stencil leaves the coarse level
+    const DevBox& O = C.box[o];
+    return v[q * C.N + O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2])];
+}
+
+__global__ void k_explode(LV F, LV C, const GhostCell* gl, long long n, const double* fc, const double* gc_,
+                          double* fg, double* gg)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const GhostCell g = gl[e];
+    const DevBox& B = F.box[g.box];
+    int fp[3] = {B.lo[0] + g.x, B.lo[1] + g.y, B.lo[2] + g.z};
+    wrap_pos(F, fp);
+    const int cp[3] = {fp[0] >> 1, fp[1] >> 1, fp[2] >> 1};
+    const double off[3] = {((fp[0] - 2 * cp[0]) + 0.5) / 2.0 - 0.5, ((fp[1] - 2 * cp[1]) + 0.5) / 2.0 - 0.5,
+                           ((fp[2] - 2 * cp[2]) + 0.5) / 2.0 - 0.5};
+    const long long gi = B.goff + fab_lin(B, g.x, g.y, g.z);
+    for (int lat = 0; lat < 2; ++lat) {
+        const double* v = lat ? gc_ : fc;
+        double* out = lat ? gg : fg;
+        double alpha[3] = {1.0, 1.0, 1.0};
+        for (int d = 0; d < 3; ++d) {
+            for (int q = 0; q < NQ; ++q) {
+                const double u0 = crse_at(C, cp, d, 0, q, v);
+                const double up = crse_at(C, cp, d, 1, q, v);
+                const double um = crse_at(C, cp, d, -1, q, v);
+                const double cen = 0.5 * (up - um);
+                const double forw = 2.0 * (up - u0);
+                const double back = 2.0 * (u0 - um);
+                const double slp = (forw * back >= 0.0) ? fmin(fabs(forw), fabs(back)) : 0.0;
+                if (cen != 0.0) alpha[d] = fmin(alpha[d], fmin(slp, fabs(cen)) / fabs(cen));
+            }
+        }
+        for (int q = 0; q < NQ; ++q) {
+            const double u0 = crse_at(C, cp, 0, 0, q, v);
+            const double cx = 0.5 * (crse_at(C, cp, 0, 1, q, v) - crse_at(C, cp, 0, -1, q, v));
+            const double cy = 0.5 * (crse_at(C, cp, 1, 1, q, v) - crse_at(C, cp, 1, -1, q, v));
+            const double cz = 0.5 * (crse_at(C, cp, 2, 1, q, v) - crse_at(C, cp, 2, -1, q, v));
+            out[q * F.NG + gi] = u0 + off[0] * (alpha[0] * cx) + off[1] * (alpha[1] * cy) + off[2] * (alpha[2] * cz);
+        }
+    }
+}
+
+// ---- coalescence: masked average of the 8 fine children --------------------
+// (masked_avgdown, Source/Utilities.H:315-350).  into_state: write into the
+// coarse state buffer directly (initial average_down, ng = 0); otherwise into
+// the coarse post-stream override buffer, with the coarse streamed value
+// where every child is masked.
+__global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, const CoalesceCell* cl, long long n,
+                           const double* ff, const double* gf, const double* ffg, const double* gfg,
+                           const double* fcA, const double* gcA, const double* fcAg, const double* gcAg,
+                           double* fcB, double* gcB, int into_state)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const CoalesceCell cc = cl[e];
+    const DevBox& O = C.box[cc.cbox];
+    const DevBox& A = F.box[cc.fbox];
+    const long long cell = O.voff + val_lin(O, cc.cx, cc.cy, cc.cz);
+    const uint8_t tf = flag_at(C, O, cc.cx, cc.cy, cc.cz);
+    const double masked = -1.0;
+    for (int lat = 0; lat < 2; ++lat) {
+        const double* v = lat ? gf : ff;
+        const double* vg = lat ? gfg : ffg;
+        double* out = lat ? gcB : fcB;
+        const double* cA = lat ? gcA : fcA;
+        const double* cAg = lat ? gcAg : fcAg;
+#define MBG_CO64(q)                                                                               \
+        {                                                                                         \
+            double s = 0.0, vol = 0.0;                                                            \
+            for (int kr = 0; kr < 2; ++kr)                                                        \
+                for (int jr = 0; jr < 2; ++jr)                                                    \
+                    for (int ir = 0; ir < 2; ++ir) {                                              \
+                        const double fv = fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg); \
+                        if (fabs(fv - masked) > ph.small_num) { s += fv; vol += 1.0; }            \
+                    }                                                                             \
+            double r;                                                                             \
+            if (vol > 0.0) r = s / vol;                                                           \
+            else if (into_state) r = cA[q * C.N + cell];                                          \
+            else r = pull<q>(C, P, O, cc.cx, cc.cy, cc.cz, tf, false, cA, cAg, lat == 1, ph.lat); \
+            out[q * C.N + cell] = r;                                                              \
+        }
+        MBG_UNROLL27(MBG_CO64)
+#undef MBG_CO64
+    }
+}
+
+void launch_explode(const LevelPlan& fine, const LevelPlan& crse, const double* fc, const double* gc, double* fg,
+                    double* gg, cudaStream_t s)
+{
+    if (fine.nghost_cells == 0) return;
+    const int th = 64;
+    const long long nb = (fine.nghost_cells + th - 1) / th;
+    k_explode<<<(unsigned)nb, th, 0, s>>>(fine.view64, crse.view64, fine.ghost_list, fine.nghost_cells, fc, gc, fg,
+                                          gg);
+}
+
+void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParams& P, const Phys64& ph,
+                     const CoalesceCell* list, long long n, const double* ff, const double* gf, const double* ffg,
+                     const double* gfg, const double* fcA, const double* gcA, const double* fcAg,
+                     const double* gcAg, double* fcB, double* gcB, int into_state, cudaStream_t s)
+{
+    if (n == 0) return;
+    const int th = 64;
+    const long long nb = (n + th - 1) / th;
+    k_coalesce<<<(unsigned)nb, th, 0, s>>>(crse.view64, fine.view64, P, ph, list, n, ff, gf, ffg, gfg, fcA, gcA,
+                                           fcAg, gcAg, fcB, gcB, into_state);
+}
+
+}  // namespace mbg

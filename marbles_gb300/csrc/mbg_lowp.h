@@ -2,6 +2,7 @@
 // step (mbg_lowp.cu).
 #pragma once
 
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -17,25 +18,29 @@ struct LowpLevel {
     void* g[2] = {nullptr, nullptr};
     void* fg[2] = {nullptr, nullptr};   // ghost fabs, [q][NG]
     void* gg[2] = {nullptr, nullptr};
-    float* qc = nullptr;                // Q_corr scratch of the two-pass kernels
-    float* gqc = nullptr;
     double* tmp = nullptr;              // FP64 staging for state transfer
     int cur = 0;
     Phys32 ph;
+    void* impl = nullptr;               // codecs, tiles, override buffers (mbg_lowp.cu)
     std::vector<void*> allocs;
 };
 
 mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::vector<DevBox>& hbox, long long N,
-                       long long NG, LowpLevel& L, std::string& err);
+                       long long NG, double dt, const double idx[3], LowpLevel& L, std::string& err);
+void lowp_release(LowpLevel& L);
 mbg_status lowp_set_state(LowpLevel& L, const LevelPlan& plan, const std::vector<DevBox>& hbox, const double* f,
                           const double* g, cudaStream_t s, std::string& err);
 mbg_status lowp_get_state(LowpLevel& L, const LevelPlan& plan, const std::vector<DevBox>& hbox, double* f,
                           double* g, cudaStream_t s, std::string& err);
 mbg_status lowp_macro(LowpLevel& L, const LevelPlan& plan, double* out19, cudaStream_t s, std::string& err);
+// Stages of one 16-bit level advance, each one kernel launch; the caller's
+// runner wraps every launch (the library times them with CUDA events).
+enum { LOWP_STAGE_COALESCE = 0, LOWP_STAGE_GHOST_STREAM, LOWP_STAGE_FUSED };
+using LowpRunner = std::function<void(int stage, const std::function<void()>& launch)>;
 // returns the number of kernels launched
 int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const LevelPlan& plan, double dt,
                  const double idx[3], const CoalesceCell* coal, long long ncoal, const LowpLevel* fine,
-                 const LevelPlan* fplan, cudaStream_t s);
+                 const LevelPlan* fplan, cudaStream_t s, const LowpRunner& run);
 void lowp_explode(LowpLevel& F, const LevelPlan& fplan, const LowpLevel& C, const LevelPlan& cplan, cudaStream_t s);
 void lowp_average_down(LowpLevel& C, const LevelPlan& cplan, const LowpLevel& F, const LevelPlan& fplan,
                        const CoalesceCell* list, long long n, cudaStream_t s);

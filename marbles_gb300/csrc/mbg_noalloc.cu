@@ -73,10 +73,9 @@ __global__ void __launch_bounds__(TILE_CELLS) k_na_moments(BoxDims b, Phys64 ph,
     long long c;
     if (!na_cell(b, x, y, z, c)) return;
     MomentAcc<double> acc;
-    static_for<0, NQ>([&](auto qc) {
-        constexpr int q = decltype(qc)::value;
-        acc.template add<q>(na_pull<q>(b, x, y, z, f), na_pull<q>(b, x, y, z, g));
-    });
+#define MBG_NAM(q) acc.template add<q>(na_pull<q>(b, x, y, z, f), na_pull<q>(b, x, y, z, g));
+    MBG_UNROLL27(MBG_NAM)
+#undef MBG_NAM
     const Macro<double> m = acc.finish(ph.mesh_speed, ph.Rg, ph.cv);
     const long long N = b.N;
     md[MD_RHO * N + c] = m.rho;
@@ -159,16 +158,20 @@ __global__ void __launch_bounds__(TILE_CELLS) k_na_collide(BoxDims b, Phys64 ph,
     Equilibrium<double> E;
     const double omega =
         build_equilibrium<double>(m, dqx, dqy, dqz, ph.nu, ph.alpha, ph.dt, ph.Rg, ph.cv, ph.lat, E);
-    static_for<0, NQ>([&](auto qc) {
-        constexpr int q = decltype(qc)::value;
-        const double fq = na_pull<q>(b, x, y, z, f);
-        fo[q * N + c] = fq + omega * (E.template feq<q>() - fq);
-    });
-    static_for<0, NQ>([&](auto qc) {
-        constexpr int q = decltype(qc)::value;
-        const double gq = na_pull<q>(b, x, y, z, g);
-        go[q * N + c] = gq + omega * (E.template geq<q>(ph.lat) - gq);
-    });
+#define MBG_NAF(q)                                                   \
+    {                                                                \
+        const double fq = na_pull<q>(b, x, y, z, f);                 \
+        fo[q * N + c] = fq + omega * (E.template feq<q>() - fq);     \
+    }
+#define MBG_NAG(q)                                                   \
+    {                                                                \
+        const double gq = na_pull<q>(b, x, y, z, g);                 \
+        go[q * N + c] = gq + omega * (E.template geq<q>(ph.lat) - gq); \
+    }
+    MBG_UNROLL27(MBG_NAF)
+    MBG_UNROLL27(MBG_NAG)
+#undef MBG_NAF
+#undef MBG_NAG
 }
 
 }  // namespace mbg

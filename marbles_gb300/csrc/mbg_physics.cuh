@@ -58,6 +58,11 @@ __host__ __device__ constexpr int ev_norm1(int q)
     return (ev_x(q) != 0) + (ev_y(q) != 0) + (ev_z(q) != 0);
 }
 
+// M(q) for q = 0 .. 26 in order, with q a literal: the unrolled direction
+// loops of the kernels (plain expansion, nothing captured)
+#define MBG_UNROLL27(M) M(0) M(1) M(2) M(3) M(4) M(5) M(6) M(7) M(8) M(9) M(10) M(11) M(12) M(13) M(14) \
+    M(15) M(16) M(17) M(18) M(19) M(20) M(21) M(22) M(23) M(24) M(25) M(26)
+
 template <int Q, int N, class F>
 __device__ __forceinline__ void static_for(F&& f)
 {

@@ -45,6 +45,9 @@ def mbg_params_from(p, precision=0):
     q.vbc_m_bar = p.vbc_m_bar
     q.rho_ref = 1.0
     q.t_ref = p.initial_temperature
+    if p.ic_type == O.IC_TYPES["constant"]:
+        sos = math.sqrt(p.ic_adiabatic_exponent * (R_U / p.ic_m_bar) * p.ic_initial_temperature)
+        q.u_ref[:] = [p.ic_mach[d] * sos for d in range(3)]
     return q
 
 

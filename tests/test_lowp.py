@@ -1,0 +1,109 @@
+"""FP32-arithmetic / 16-bit-storage forms against the FP64 path (GPU).
+
+The FP64 path is bit-identical to the oracle on these cases
+(test_parity_fp64.py), so its state stands in for the oracle's.  Errors are
+relative: rho and T pointwise, u against the largest velocity of the level.
+"""
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+# tolerances per form after the stated steps (FP16 keeps 11 significant bits
+# of the deviation from the rest state, BF16 8)
+TOL = {1: {"rho": 1e-4, "u": 1e-2, "T": 1e-4}, 2: {"rho": 1e-3, "u": 8e-2, "T": 1e-3}}
+
+
+def _pair(p, levels, prec):
+    import marbles_gb300 as M
+    o = cases.run_oracle(p, levels, 0)
+    c64 = M.Context(cases.mbg_params_from(p, 0))
+    c16 = M.Context(cases.mbg_params_from(p, prec))
+    for lev, b in enumerate(levels):
+        fl = o.get_grown_flags(lev)
+        f, g = o.get_state(lev)
+        c64.define_level(lev, b, fl)
+        c16.define_level(lev, b, fl)
+        c64.set_state(lev, f, g)
+        c16.set_state(lev, f, g)
+    return c64, c16
+
+
+def _errors(c64, c16, levels):
+    worst = {"rho": 0.0, "u": 0.0, "T": 0.0}
+    for lev in range(len(levels)):
+        a = c16.get_macro(lev)
+        r = c64.get_macro(lev)
+        assert np.isfinite(a).all()
+        off = 0
+        for b in levels[lev]:
+            vol = int(np.prod(b[3:] - b[:3] + 1))
+            A = a[off:off + 19 * vol].reshape(19, vol)
+            R = r[off:off + 19 * vol].reshape(19, vol)
+            off += 19 * vol
+            fluid = R[0] != 0
+            worst["rho"] = max(worst["rho"], float(np.max(np.abs(A[0] - R[0])[fluid] / R[0][fluid])))
+            worst["T"] = max(worst["T"], float(np.max(np.abs(A[18] - R[18])[fluid] / R[18][fluid])))
+            umax = max(float(np.max(np.abs(R[1:4]))), 1e-30)
+            worst["u"] = max(worst["u"], float(np.max(np.abs(A[1:4] - R[1:4]))) / umax)
+    return worst
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_taylor_green(prec):
+    p, levels = cases.taylor_green(32, 16, nu=0.1733333333333333)
+    c64, c16 = _pair(p, levels, prec)
+    c64.step(50)
+    c16.step(50)
+    e = _errors(c64, c16, levels)
+    assert all(e[k] <= TOL[prec][k] for k in e), e
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_sphere_inflow_outflow(prec):
+    p, levels = cases.sphere_channel(64, 32, 32, radius=6.0, center=(20.0, 16.0, 16.0), mgs=16, t0=0.03)
+    c64, c16 = _pair(p, levels, prec)
+    c64.step(40)
+    c16.step(40)
+    e = _errors(c64, c16, levels)
+    assert all(e[k] <= TOL[prec][k] for k in e), e
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_two_level_pulse(prec):
+    p, levels = cases.gaussian_pulse(nc=32, fine_lo=8, fine_hi=23, mgs=16, width=3.0, t0=0.1)
+    c64, c16 = _pair(p, levels, prec)
+    c64.step(20)
+    c16.step(20)
+    e = _errors(c64, c16, levels)
+    assert all(e[k] <= TOL[prec][k] for k in e), e
+
+
+def test_three_level_sphere_fp16():
+    p, levels = cases.sphere_channel(64, 32, 32, radius=5.0, center=(24.0, 16.0, 16.0), mgs=16, levels=3, t0=0.03)
+    c64, c16 = _pair(p, levels, 1)
+    c64.step(5)
+    c16.step(5)
+    e = _errors(c64, c16, levels)
+    assert all(e[k] <= TOL[1][k] for k in e), e
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_state_round_trip_and_sentinel(prec):
+    """Upload then download: values within the format's rounding, solid
+    cells' -1 sentinel kept exactly."""
+    p, levels = cases.sphere_channel(32, 16, 16, radius=4.0, center=(12.0, 8.0, 8.0), mgs=16, t0=0.03)
+    import marbles_gb300 as M
+    o = cases.run_oracle(p, levels, 1)        # after one step solid cells hold -1
+    c16 = M.Context(cases.mbg_params_from(p, prec))
+    c16.define_level(0, levels[0], o.get_grown_flags(0))
+    f, g = o.get_state(0)
+    c16.set_state(0, f, g)
+    f2, g2 = c16.get_state(0)
+    sent = f == -1.0
+    assert sent.any() and (f2[sent] == -1.0).all()
+    eps = 2.0 ** -11 if prec == 1 else 2.0 ** -8
+    live = ~sent
+    assert np.max(np.abs(f2[live] - f[live]) / np.abs(f[live])) < 4 * eps
