@@ -23,6 +23,8 @@ UNITS = {
     "mbg_fp64_amr.cu": ["-fmad=false"],
     "mbg_fp64_out.cu": ["-fmad=false"],
     "mbg_lowp.cu": [],
+    "mbg_lowp_f16.cu": [],
+    "mbg_lowp_bf16.cu": [],
     "mbg_capi.cu": [],
     "lbm_driver.cu": [],
     "lbm_capi.cu": [],

@@ -70,9 +70,9 @@ struct Level {
 }  // namespace
 
 // kernel classes timed by mbg_set_timing
-enum { TK_MOMENTS = 0, TK_COLLIDE, TK_GHOST_STREAM, TK_GHOST_MOMENTS, TK_EXPLODE, TK_COALESCE, TK_FUSED, TK_OTHER, TK_N };
+enum { TK_MOMENTS = 0, TK_COLLIDE, TK_GHOST_STREAM, TK_GHOST_MOMENTS, TK_EXPLODE, TK_COALESCE, TK_FUSED, TK_HALO, TK_OTHER, TK_N };
 static const char* TK_NAMES[TK_N] = {"k_moments", "k_collide", "k_ghost_stream", "k_ghost_moments",
-                                     "k_explode", "k_coalesce", "k_lowp_fused", "other"};
+                                     "k_explode", "k_coalesce", "k_lowp_fused", "k_halo", "other"};
 
 struct mbg_ctx {
     mbg_params p;
@@ -405,9 +405,14 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     for (int n = 0; n < nbox; ++n) {
         DevBox& B = L.hbox[n];
         for (int d = 0; d < 3; ++d) { B.lo[d] = L.boxes[n].lo[d]; B.n[d] = L.boxes[n].n(d); }
+        B.sy = B.n[0];
+        B.sz = B.n[0] * B.n[1];
         B.voff = voff;
+        B.hoff = voff;
         B.foff = foff;
         B.goff = -1;
+        B.phys = 0;
+        B.pad = 0;
         voff += L.boxes[n].vol();
         foff += L.boxes[n].gvol();
     }
@@ -422,6 +427,15 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
         B.all_fluid = 1;
         for (long long i = 0; i < L.boxes[n].gvol(); ++i)
             if (!(L.hflags[B.foff + i] & FL_FLUID)) { B.all_fluid = 0; break; }
+        B.vfluid = 1;
+        for (int z = -1; z <= B.n[2] && B.vfluid; ++z)
+            for (int y = -1; y <= B.n[1] && B.vfluid; ++y)
+                for (int x = -1; x <= B.n[0]; ++x)
+                    if (!(L.hflags[B.foff + ((long long)(z + 3) * (B.n[1] + 6) + (y + 3)) * (B.n[0] + 6) + (x + 3)] &
+                          FL_FLUID)) {
+                        B.vfluid = 0;
+                        break;
+                    }
     }
     // coarse-fine ghost shell of fine levels
     std::vector<GhostCell> ghosts, ghosts1;
@@ -682,7 +696,7 @@ static mbg_status advance(mbg_ctx* ctx, int lev)
         const LowpLevel* fine = has_finer ? &ctx->lv[lev + 1].lowp : nullptr;
         const LevelPlan* fplan = has_finer ? &ctx->lv[lev + 1].plan : nullptr;
         int nl = 0;
-        static const int stage_tk[3] = {TK_COALESCE, TK_GHOST_STREAM, TK_FUSED};
+        static const int stage_tk[4] = {TK_COALESCE, TK_GHOST_STREAM, TK_FUSED, TK_HALO};
         nl = lowp_advance(ctx->p, ctx->bc, L.lowp, L.plan, L.dt, L.idx, has_finer ? L.d_coal1 : nullptr,
                           has_finer ? L.ncoal1 : 0, fine, fplan, ctx->s,
                           [&](int stage, const std::function<void()>& launch) { timed(ctx, stage_tk[stage], launch); });

@@ -17,7 +17,7 @@ __global__ void k_macro_local(LV L, Phys64 ph, const Tile* tiles, const double* 
     const long long N = L.N;
     // host layout [box][comp][cell]
     const long long vol = (long long)B.n[0] * B.n[1] * B.n[2];
-    double* o = out19 + B.voff * 19 + c;
+    double* o = out19 + B.hoff * 19 + c;
     if (!(flag_at(L, B, x, y, z) & FL_FLUID)) {
         for (int k = 0; k < 19; ++k) o[k * vol] = 0.0;
         return;

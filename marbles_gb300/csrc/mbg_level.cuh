@@ -3,8 +3,11 @@
 //
 // Layout in HBM (per level):
 //   * populations of valid cells, component-major over the whole level:
-//       v[q * N + voff(box) + (k * ny + j) * nx + i]
-//     (each box's valid cells are contiguous; no ghost copies are stored)
+//       v[q * N + voff(box) + k * sz + j * sy + i]
+//     The FP64 form stores valid cells only (sy = nx, sz = nx ny, each box
+//     contiguous); the 16-bit form pads every box by one cell on each side
+//     (sy = nx + 2, sz = (nx + 2)(ny + 2)) and fills the pad with the
+//     streamed values that cross the box faces.
 //   * for fine levels, a private ghost fab per box (the box grown by 3),
 //     used only at cells no valid box of the level covers (the coarse-fine
 //     ghost shell):  vg[q * NG + goff(box) + ((k+3)(ny+6) + (j+3))(nx+6) + (i+3)]
@@ -37,10 +40,14 @@ enum : uint8_t { FL_FLUID = 1, FL_EBB = 2, FL_OVR = 4 };
 struct DevBox {
     int lo[3];
     int n[3];
-    long long voff;   // first valid cell of the box in level cell order
+    int sy, sz;       // strides of the box's cell array along y and z
+    long long voff;   // storage index of the box's valid cell (0,0,0)
+    long long hoff;   // first valid cell of the box in host (level cell) order
     long long foff;   // first cell of the box's grown flag fab
     long long goff;   // first cell of the box's grown ghost fab (-1: none)
     int all_fluid;    // no solid cell anywhere in the grown fab
+    int vfluid;       // every cell of the box grown by one is fluid
+    int phys;         // index of the box's physical parameters (batched domains)
     int pad;
 };
 
@@ -70,9 +77,11 @@ __device__ __forceinline__ long long fab_lin(const DevBox& B, int x, int y, int 
 {
     return ((long long)(z + 3) * (B.n[1] + 6) + (y + 3)) * (B.n[0] + 6) + (x + 3);
 }
+// storage offset of box-local (x,y,z) from the box's valid origin; with
+// unpadded strides (sy = nx, sz = nx ny) this is the valid-cell order
 __device__ __forceinline__ long long val_lin(const DevBox& B, int x, int y, int z)
 {
-    return ((long long)z * B.n[1] + y) * B.n[0] + x;
+    return (long long)z * B.sz + (long long)y * B.sy + x;
 }
 
 template <class S>

@@ -13,12 +13,13 @@ namespace mbg {
 
 struct LowpLevel {
     int precision = 0;           // MBG_FP32C_F16S or MBG_FP32C_BF16S
-    long long N = 0, NG = 0;
+    long long N = 0, NG = 0;            // storage cells (valid + one-cell pad per box), ghost-fab cells
+    long long NV = 0;                   // valid cells
     void* f[2] = {nullptr, nullptr};    // 16-bit populations, [q][N]
     void* g[2] = {nullptr, nullptr};
     void* fg[2] = {nullptr, nullptr};   // ghost fabs, [q][NG]
     void* gg[2] = {nullptr, nullptr};
-    double* tmp = nullptr;              // FP64 staging for state transfer
+    double* tmp = nullptr;              // FP64 staging for state transfer, [q][NV]
     int cur = 0;
     Phys32 ph;
     void* impl = nullptr;               // codecs, tiles, override buffers (mbg_lowp.cu)
@@ -35,7 +36,7 @@ mbg_status lowp_get_state(LowpLevel& L, const LevelPlan& plan, const std::vector
 mbg_status lowp_macro(LowpLevel& L, const LevelPlan& plan, double* out19, cudaStream_t s, std::string& err);
 // Stages of one 16-bit level advance, each one kernel launch; the caller's
 // runner wraps every launch (the library times them with CUDA events).
-enum { LOWP_STAGE_COALESCE = 0, LOWP_STAGE_GHOST_STREAM, LOWP_STAGE_FUSED };
+enum { LOWP_STAGE_COALESCE = 0, LOWP_STAGE_GHOST_STREAM, LOWP_STAGE_FUSED, LOWP_STAGE_HALO };
 using LowpRunner = std::function<void(int stage, const std::function<void()>& launch)>;
 // returns the number of kernels launched
 int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const LevelPlan& plan, double dt,

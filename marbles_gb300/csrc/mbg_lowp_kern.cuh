@@ -1,0 +1,706 @@
+// mbg_lowp_kern.cuh -- kernels of the FP32-arithmetic / 16-bit-storage form of
+// the level step, compiled once per storage format (mbg_lowp_f16.cu,
+// mbg_lowp_bf16.cu); the host side is mbg_lowp.cu.
+//
+// Storage.  Each population is kept as a 16-bit float (FP16 or BF16) holding
+// its scaled deviation from the equilibrium at the reference state
+// (rho_ref, u_ref, T_ref):  f = f_rest[q] + scale[q] * h.  scale[q] is the rest
+// value itself for f (h is then the relative deviation) and the rest value of
+// g floored at 1e-3 w_q (2 rho E)_ref (g_rest vanishes for some directions).
+// The stream's -1 sentinel (solid cells, unreached ghosts) is the code 0xFFFF,
+// a NaN in both formats, decoded to exactly -1.
+//
+// Layout.  Every box is stored padded by one cell on each side,
+// component-major over the level: v[q * N + voff + z sz + y sy + x] with
+// sy = nx + 2, sz = (nx + 2)(ny + 2).  Before each advance k_halo16 writes
+// into the pad of the source buffer, for every direction q that crosses a box
+// face, the exact value the pull of the cell behind that face must see: the
+// neighbour box's value (periodic images included), the physical-BC value,
+// the coarse-fine ghost value, the bounce-back value or the -1 sentinel.
+// The step kernel then pulls every direction by index arithmetic alone.
+//
+// Arithmetic.  FP32 throughout the collision; FP64 only where sums of many
+// terms meet: the coalescence averages and the output moments.
+//
+// One level advance is one fused pass (k_fused): a CTA owns a tw x (256/tw)
+// column tile of a box (tw = 8, 16 or 32) and marches through a run of planes.
+// For each plane it pulls the 54 streamed values of its cells, forms the
+// moments and Q_corr, and keeps Q_corr of the tile plus a one-cell halo in
+// shared memory (halo cells are computed from the perspective of the box
+// that owns them, so the coarse-fine ghost semantics match the reference);
+// the previous plane is then collided: q-correction gradient from shared
+// memory, equilibria, relaxation, with its 54 values pulled again from L1/L2.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "mbg_lowp_types.cuh"
+
+namespace mbg {
+
+template <bool BF>
+__device__ __forceinline__ float h2f(u16 r)
+{
+    if constexpr (BF) return __uint_as_float(((unsigned)r) << 16);
+    else return __half2float(__ushort_as_half(r));
+}
+template <bool BF>
+__device__ __forceinline__ u16 f2h(float v)
+{
+    if constexpr (BF) return __bfloat16_as_ushort(__float2bfloat16_rn(v));
+    else return __half_as_ushort(__float2half_rn(v));
+}
+template <bool BF>
+__device__ __forceinline__ float dec(const CodecTab& ct, u16 r, int q, bool g)
+{
+    if (r == SENT16) return -1.0f;
+    return g ? fmaf(h2f<BF>(r), ct.gsc[q], ct.grest[q]) : fmaf(h2f<BF>(r), ct.fsc[q], ct.frest[q]);
+}
+template <bool BF>
+__device__ __forceinline__ u16 enc(const CodecTab& ct, float v, int q, bool g)
+{
+    if (v == -1.0f) return SENT16;
+    const float h = g ? (v - ct.grest[q]) * ct.gisc[q] : (v - ct.frest[q]) * ct.fisc[q];
+    const u16 r = f2h<BF>(h);
+    return r == SENT16 ? (u16)0xFFFEu : r;
+}
+
+
+
+// general pull (everything but an interior cell of an all-fluid box), the
+// 16-bit counterpart of mbg_fp64.cu's pull; which: bit 0 = g lattice
+template <int q, bool BF>
+__device__ __noinline__ float pull16_slow(const LowpK* __restrict__ K, int b, int x, int y, int z, uint8_t tflag,
+                                          int which)
+{
+    constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
+    constexpr int oq = opp(q);
+    const bool is_g = which & 1;
+    const u16* v = is_g ? K->s.g : K->s.f;
+    const u16* vg = is_g ? K->s.gg : K->s.fg;
+    const LV16& L = K->L;
+    const DevBox& B = L.box[b];
+    if (!(tflag & FL_FLUID)) return -1.0f;
+    const int sx = x - ex, sy = y - ey, sz = z - ez;
+    if (sx < -3 || sy < -3 || sz < -3 || sx > B.n[0] + 2 || sy > B.n[1] + 2 || sz > B.n[2] + 2) return -1.0f;
+    const uint8_t sf = flag_at(L, B, sx, sy, sz);
+    if (!(sf & FL_FLUID)) return dec<BF>(K->ct, fab_value(L, B, x, y, z, oq, v, vg), oq, is_g);
+    int gp[3] = {B.lo[0] + sx, B.lo[1] + sy, B.lo[2] + sz};
+    if (outside_nonperiodic(L, gp))
+        return bc_value<q, u16, float>(L, K->P, B, sx, sy, sz, is_g, v, vg, K->lat64,
+                                       [&](u16 r, int slot) { return dec<BF>(K->ct, r, slot, is_g); });
+    return dec<BF>(K->ct, fab_value(L, B, sx, sy, sz, q, v, vg), q, is_g);
+}
+
+// moments of the streamed values at box-local (x, y, z) of box b; a cell
+// overwritten by coalescence reads the override buffer instead
+template <bool BF>
+__device__ __noinline__ MomentAcc<float> moments16_slow(const LowpK* __restrict__ K, int b, int x, int y, int z,
+                                                        uint8_t tf)
+{
+    MomentAcc<float> acc;
+    const LV16& L = K->L;
+    const DevBox& B = L.box[b];
+    const bool ovr = (tf & FL_OVR) && in_valid<u16>(B, x, y, z) && K->s.fo;
+    const long long cell = B.voff + (in_valid<u16>(B, x, y, z) ? val_lin(B, x, y, z) : 0);
+#define MBG_MS16(q)                                                                  \
+    {                                                                                \
+        float fq, gq;                                                                \
+        if (ovr) {                                                                   \
+            fq = dec<BF>(K->ct, K->s.fo[q * L.N + cell], q, false);                  \
+            gq = dec<BF>(K->ct, K->s.go[q * L.N + cell], q, true);                   \
+        } else {                                                                     \
+            fq = pull16_slow<q, BF>(K, b, x, y, z, tf, 0);                           \
+            gq = pull16_slow<q, BF>(K, b, x, y, z, tf, 1);                           \
+        }                                                                            \
+        acc.template add<q>(fq, gq);                                                 \
+    }
+    MBG_UNROLL27(MBG_MS16)
+#undef MBG_MS16
+    return acc;
+}
+
+// raw code of the value the pull of direction q at target (x,y,z) of box b
+// sees; computed values (physical BCs) are encoded, stored ones copied
+template <int q, bool BF>
+__device__ __noinline__ u16 pull16_code(const LowpK* __restrict__ K, int b, int x, int y, int z, uint8_t tflag,
+                                        int which)
+{
+    constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
+    const bool is_g = which & 1;
+    const u16* v = is_g ? K->s.g : K->s.f;
+    const u16* vg = is_g ? K->s.gg : K->s.fg;
+    const LV16& L = K->L;
+    const DevBox& B = L.box[b];
+    if (!(tflag & FL_FLUID)) return SENT16;
+    const int sx = x - ex, sy = y - ey, sz = z - ez;
+    if (sx < -3 || sy < -3 || sz < -3 || sx > B.n[0] + 2 || sy > B.n[1] + 2 || sz > B.n[2] + 2) return SENT16;
+    // a solid source bounces back; the step kernel does that itself from the
+    // target's own opposite population, so the pad value is never read
+    const uint8_t sf = flag_at(L, B, sx, sy, sz);
+    if (!(sf & FL_FLUID)) return SENT16;
+    int gp[3] = {B.lo[0] + sx, B.lo[1] + sy, B.lo[2] + sz};
+    if (outside_nonperiodic(L, gp))
+        return enc<BF>(K->ct,
+                       bc_value<q, u16, float>(L, K->P, B, sx, sy, sz, is_g, v, vg, K->lat64,
+                                               [&](u16 r, int slot) { return dec<BF>(K->ct, r, slot, is_g); }),
+                       q, is_g);
+    return fab_value(L, B, sx, sy, sz, q, v, vg);
+}
+
+
+// fill the pad of the source buffer: for every direction q whose pull from
+// the pad cell lands in the box, the value that pull must see
+template <bool BF>
+__global__ void k_halo16(const LowpK* __restrict__ K, const HaloCell* __restrict__ hl, long long n)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const HaloCell h = hl[e];
+    const LV16& L = K->L;
+    const DevBox& B = L.box[h.box];
+    const long long hc = B.voff + val_lin(B, h.x, h.y, h.z);
+#define MBG_HF16(q)                                                                                      \
+    {                                                                                                    \
+        const int tx = h.x + ev_x(q), ty = h.y + ev_y(q), tz = h.z + ev_z(q);                            \
+        if (in_valid<u16>(B, tx, ty, tz)) {                                                              \
+            const uint8_t tf = flag_at(L, B, tx, ty, tz);                                                \
+            K->fA[q * L.N + hc] = pull16_code<q, BF>(K, h.box, tx, ty, tz, tf, 0);                       \
+            K->gA[q * L.N + hc] = pull16_code<q, BF>(K, h.box, tx, ty, tz, tf, 1);                       \
+        }                                                                                                \
+    }
+    MBG_UNROLL27(MBG_HF16)
+#undef MBG_HF16
+}
+
+// pad of self-periodic boxes (batched independent domains): a copy of the
+// opposite face, edge or corner of the same box
+template <bool BF>
+__global__ void k_halo_periodic16(const LowpK* __restrict__ K, const HaloCell* __restrict__ hl, long long n)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const HaloCell h = hl[e];
+    const LV16& L = K->L;
+    const DevBox& B = L.box[h.box];
+    const long long hc = B.voff + val_lin(B, h.x, h.y, h.z);
+    const int wx = h.x < 0 ? B.n[0] - 1 : h.x >= B.n[0] ? 0 : h.x;
+    const int wy = h.y < 0 ? B.n[1] - 1 : h.y >= B.n[1] ? 0 : h.y;
+    const int wz = h.z < 0 ? B.n[2] - 1 : h.z >= B.n[2] ? 0 : h.z;
+    const long long sc = B.voff + val_lin(B, wx, wy, wz);
+#define MBG_HP16(q)                                                                  \
+    if (in_valid<u16>(B, h.x + ev_x(q), h.y + ev_y(q), h.z + ev_z(q))) {             \
+        K->fA[q * L.N + hc] = K->s.f[q * L.N + sc];                                  \
+        K->gA[q * L.N + hc] = K->s.g[q * L.N + sc];                                  \
+    }
+    MBG_UNROLL27(MBG_HP16)
+#undef MBG_HP16
+}
+
+// pull of direction q at valid cell c = (x,y,z) of box B from the padded
+// storage: a solid source (in the box or in its pad) bounces back, any other
+// source holds the streamed value; vf: the box grown by one is all fluid
+template <int q, bool BF>
+__device__ __forceinline__ float pullp(const CodecTab& ct, const LV16& L, const DevBox& B, const u16* __restrict__ v,
+                                       long long c, int x, int y, int z, bool vf, bool is_g)
+{
+    constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
+    if (!vf && !(flag_at(L, B, x - ex, y - ey, z - ez) & FL_FLUID))
+        return dec<BF>(ct, v[opp(q) * L.N + c], opp(q), is_g);
+    return dec<BF>(ct, __ldg(v + q * L.N + c - ((long long)ez * B.sz + (long long)ey * B.sy + ex)), q, is_g);
+}
+
+// uniform pull (every cell of the box grown by one is fluid)
+template <int q, bool BF>
+__device__ __forceinline__ float pullu(const CodecTab& ct, const u16* __restrict__ v, long long N, long long c,
+                                       int sy, int sz, bool is_g)
+{
+    constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
+    return dec<BF>(ct, __ldg(v + q * N + c - ((long long)ez * sz + (long long)ey * sy + ex)), q, is_g);
+}
+
+// moments of the streamed values at valid fluid cell (x,y,z) of box b
+template <bool BF>
+__device__ __noinline__ MomentAcc<float> moments_cell(const LowpK* __restrict__ K, int b, int x, int y, int z,
+                                                      uint8_t tf)
+{
+    const LV16& L = K->L;
+    const DevBox& B = L.box[b];
+    const long long c = B.voff + val_lin(B, x, y, z);
+    const CodecTab& ct = K->ct;
+    MomentAcc<float> acc;
+    if ((tf & FL_OVR) && K->s.fo) {
+#define MBG_MO16(q) \
+    acc.template add<q>(dec<BF>(ct, K->s.fo[q * L.N + c], q, false), dec<BF>(ct, K->s.go[q * L.N + c], q, true));
+        MBG_UNROLL27(MBG_MO16)
+#undef MBG_MO16
+        return acc;
+    }
+    const bool vf = B.vfluid;
+#define MBG_MC16(q)                                                                     \
+    acc.template add<q>(pullp<q, BF>(ct, L, B, K->s.f, c, x, y, z, vf, false),          \
+                        pullp<q, BF>(ct, L, B, K->s.g, c, x, y, z, vf, true));
+    MBG_UNROLL27(MBG_MC16)
+#undef MBG_MC16
+    return acc;
+}
+
+// Q_corr component d at box-local position (x, y, z) of box b, as the
+// reference's macro FillBoundary leaves it: computed by the box that owns the
+// cell, or by box b itself where no box covers it
+template <bool BF>
+__device__ __noinline__ float qcorr16(const LowpK* __restrict__ K, int b, int x, int y, int z, int d)
+{
+    const LV16& L = K->L;
+    const DevBox& B = L.box[b];
+    const float ms = K->ph.mesh_speed, Rg = K->ph.Rg, cv = K->ph.cv;
+    int vb = b, lx = x, ly = y, lz = z;
+    if (!in_valid<u16>(B, x, y, z)) {
+        int p[3] = {B.lo[0] + x, B.lo[1] + y, B.lo[2] + z};
+        if (!wrap_pos(L, p)) return 0.0f;
+        const int o = owner_of(L, p);
+        if (o < 0) {
+            // coarse-fine ghost: streamed values of the box's own ghost fab
+            const uint8_t tf = flag_at(L, B, x, y, z);
+            if (!(tf & FL_FLUID)) return 0.0f;
+            const Macro<float> m = moments16_slow<BF>(K, b, x, y, z, tf).finish(ms, Rg, cv);
+            return d == 0 ? m.qcx : d == 1 ? m.qcy : m.qcz;
+        }
+        vb = o;
+        const DevBox& O = L.box[o];
+        lx = p[0] - O.lo[0];
+        ly = p[1] - O.lo[1];
+        lz = p[2] - O.lo[2];
+    }
+    const uint8_t tf = flag_at(L, L.box[vb], lx, ly, lz);
+    if (!(tf & FL_FLUID)) return 0.0f;
+    const Macro<float> m = moments_cell<BF>(K, vb, lx, ly, lz, tf).finish(ms, Rg, cv);
+    return d == 0 ? m.qcx : d == 1 ? m.qcy : m.qcz;
+}
+
+// pull for the collision of a cell that is not on the uniform path
+template <int q, bool BF>
+__device__ __noinline__ float pull_gen(const LowpK* __restrict__ K, int b, int x, int y, int z, int which)
+{
+    const LV16& L = K->L;
+    const DevBox& B = L.box[b];
+    const long long c = B.voff + val_lin(B, x, y, z);
+    const bool is_g = which & 1;
+    const uint8_t tf = flag_at(L, B, x, y, z);
+    if ((tf & FL_OVR) && K->s.fo) return dec<BF>(K->ct, (is_g ? K->s.go : K->s.fo)[q * L.N + c], q, is_g);
+    return pullp<q, BF>(K->ct, L, B, is_g ? K->s.g : K->s.f, c, x, y, z, B.vfluid, is_g);
+}
+
+
+// neighbour along d is part of the gradient stencil (Utilities.H:279-312)
+__device__ __forceinline__ bool present(const LV16& L, const DevBox& B, int x, int y, int z, int d, int s)
+{
+    int p[3] = {x, y, z};
+    p[d] += s;
+    const int gd = B.lo[d] + p[d];
+    if (gd < L.dlo[d] || gd > L.dhi[d]) return false;
+    return flag_at(L, B, p[0], p[1], p[2]) & FL_FLUID;
+}
+
+__device__ __forceinline__ float grad1(bool pin, bool min, float vpv, float vcv, float vmv, float idx)
+{
+    float vp = 0.f, vc = 0.f, vm = 0.f;
+    if (!pin && !min) {
+    } else if (!pin) {
+        vc = vcv; vm = -vmv;
+    } else if (!min) {
+        vp = vpv; vc = -vcv;
+    } else {
+        vp = 0.5f * vpv; vm = -0.5f * vmv;
+    }
+    return (vp + vc + vm) * idx;
+}
+
+// One fused step over a list of tiles; a persistent grid strides through it.
+template <bool BF>
+__global__ void __launch_bounds__(FT_THREADS, 2)
+    k_fused(const LowpK* __restrict__ K, const CodecTab ct, const Lattice<float> lat,
+            const FusedTile* __restrict__ tiles, int ntiles)
+{
+    __shared__ float sqx[2][FT_QX];
+    __shared__ float sqy[2][FT_QY];
+    __shared__ float sqz[3][FT_THREADS];
+    const LV16& L = K->L;
+    const long long N = L.N;
+    const u16* __restrict__ sf = K->s.f;
+    const u16* __restrict__ sg = K->s.g;
+    const u16* __restrict__ sfo = K->s.fo;
+    const u16* __restrict__ sgo = K->s.go;
+    u16* __restrict__ fB = K->fB;
+    u16* __restrict__ gB = K->gB;
+    const float ms = K->ph.mesh_speed, Rg = K->ph.Rg, cv = K->ph.cv;
+    const int tid = threadIdx.x;
+    for (int ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+        const FusedTile t = tiles[ti];
+        const DevBox& B = L.box[t.box];
+        const int n0 = B.n[0], n1 = B.n[1], n2 = B.n[2], sy = B.sy, sz = B.sz;
+        const long long voff = B.voff;
+        const bool vf = B.vfluid;
+        const Phys32* __restrict__ PH = K->phys ? K->phys + B.phys : &K->ph;
+        const float nu = PH->nu, alpha = PH->alpha, dt = PH->dt;
+        const float idx0 = PH->idx[0], idx1 = PH->idx[1], idx2 = PH->idx[2];
+        const int lgw = t.lgw, tw = 1 << lgw, th = FT_THREADS >> lgw;
+        const int lx = tid & (tw - 1), ly = tid >> lgw;
+        const int x = t.x0 + lx, y = t.y0 + ly;
+        const bool mine = x < n0 && y < n1;
+        const int twe = n0 - t.x0 < tw ? n0 - t.x0 : tw, the = n1 - t.y0 < th ? n1 - t.y0 : th;
+        const int px = tw + 2;   // row pitch of sqx
+        const int z0 = t.z0, z1 = t.z1;
+        Macro<float> prev, cur;
+        uint8_t prevf = 0, curf = 0;
+        for (int z = z0 - 1; z <= z1; ++z) {
+            // ---- phase A: moments and Q_corr of plane z ----
+            const int ia = z & 1, iz = (z + 3) % 3;
+            if (mine) {
+                if (z >= z0 && z < z1) {
+                    const uint8_t tf = flag_at(L, B, x, y, z);
+                    float qx = 0.f, qy = 0.f, qz = 0.f;
+                    if (tf & FL_FLUID) {
+                        MomentAcc<float> acc;
+                        if (vf && !((tf & FL_OVR) && sfo)) {
+                            const long long c = voff + (long long)z * sz + (long long)y * sy + x;
+#define MBG_MF16(q) \
+    acc.template add<q>(pullu<q, BF>(ct, sf, N, c, sy, sz, false), pullu<q, BF>(ct, sg, N, c, sy, sz, true));
+                            MBG_UNROLL27(MBG_MF16)
+#undef MBG_MF16
+                        } else {
+                            acc = moments_cell<BF>(K, t.box, x, y, z, tf);
+                        }
+                        cur = acc.finish(ms, Rg, cv);
+                        qx = cur.qcx; qy = cur.qcy; qz = cur.qcz;
+                    }
+                    curf = tf;
+                    sqx[ia][ly * px + lx + 1] = qx;
+                    sqy[ia][(ly + 1) * tw + lx] = qy;
+                    sqz[iz][tid] = qz;
+                } else {
+                    // z-halo plane: Q_corr_z only, where the gradient will read it
+                    const int zz = z < z0 ? z0 : z1 - 1;
+                    const int s_ = z < z0 ? -1 : 1;
+                    float v = 0.f;
+                    if (present(L, B, x, y, zz, 2, s_)) v = qcorr16<BF>(K, t.box, x, y, z, 2);
+                    sqz[iz][tid] = v;
+                }
+            }
+            if (z >= z0 && z < z1) {
+                // x- and y-halo of the tile in this plane
+                const int nh = 2 * the + 2 * twe;
+                for (int h = tid; h < nh; h += FT_THREADS) {
+                    if (h < 2 * the) {
+                        const int j = h >> 1, side = h & 1;
+                        const int hx = side ? t.x0 + twe : t.x0 - 1, hy = t.y0 + j;
+                        float v = 0.f;
+                        if (present(L, B, side ? hx - 1 : hx + 1, hy, z, 0, side ? 1 : -1))
+                            v = qcorr16<BF>(K, t.box, hx, hy, z, 0);
+                        sqx[ia][j * px + (side ? twe + 1 : 0)] = v;
+                    } else {
+                        const int k = h - 2 * the;
+                        const int i = k >> 1, side = k & 1;
+                        const int hx = t.x0 + i, hy = side ? t.y0 + the : t.y0 - 1;
+                        float v = 0.f;
+                        if (present(L, B, hx, side ? hy - 1 : hy + 1, z, 1, side ? 1 : -1))
+                            v = qcorr16<BF>(K, t.box, hx, hy, z, 1);
+                        sqy[ia][(side ? the + 1 : 0) * tw + i] = v;
+                    }
+                }
+            }
+            __syncthreads();
+            // ---- phase B: collide plane z - 1 ----
+            const int zc = z - 1;
+            if (mine && zc >= z0 && zc < z1) {
+                const int ib = zc & 1;
+                const long long c = voff + (long long)zc * sz + (long long)y * sy + x;
+                const bool ovr = (prevf & FL_OVR) && sfo;
+                if (!(prevf & FL_FLUID)) {
+#define MBG_SOL16(q)                                                \
+    {                                                               \
+        fB[q * N + c] = ovr ? sfo[q * N + c] : SENT16;              \
+        gB[q * N + c] = ovr ? sgo[q * N + c] : SENT16;              \
+    }
+                    MBG_UNROLL27(MBG_SOL16)
+#undef MBG_SOL16
+                } else {
+                    const float dqx = grad1(present(L, B, x, y, zc, 0, 1), present(L, B, x, y, zc, 0, -1),
+                                            sqx[ib][ly * px + lx + 2], sqx[ib][ly * px + lx + 1],
+                                            sqx[ib][ly * px + lx], idx0);
+                    const float dqy = grad1(present(L, B, x, y, zc, 1, 1), present(L, B, x, y, zc, 1, -1),
+                                            sqy[ib][(ly + 2) * tw + lx], sqy[ib][(ly + 1) * tw + lx],
+                                            sqy[ib][ly * tw + lx], idx1);
+                    const float dqz = grad1(present(L, B, x, y, zc, 2, 1), present(L, B, x, y, zc, 2, -1),
+                                            sqz[(z + 3) % 3][tid], sqz[(zc + 3) % 3][tid],
+                                            sqz[(zc - 1 + 3) % 3][tid], idx2);
+                    Equilibrium<float> E;
+                    const float omega = build_equilibrium<float>(prev, dqx, dqy, dqz, nu, alpha, dt, Rg, cv, lat, E);
+                    if (vf && !ovr) {
+#define MBG_RI16(q)                                                                                  \
+    {                                                                                                \
+        const float fq = pullu<q, BF>(ct, sf, N, c, sy, sz, false);                                  \
+        fB[q * N + c] = enc<BF>(ct, fmaf(omega, E.template feq<q>() - fq, fq), q, false);            \
+        const float gq = pullu<q, BF>(ct, sg, N, c, sy, sz, true);                                   \
+        gB[q * N + c] = enc<BF>(ct, fmaf(omega, E.template geq<q>(lat) - gq, gq), q, true);          \
+    }
+                        MBG_UNROLL27(MBG_RI16)
+#undef MBG_RI16
+                    } else {
+#define MBG_RS16(q)                                                                                  \
+    {                                                                                                \
+        const float fq = pull_gen<q, BF>(K, t.box, x, y, zc, 0);                                     \
+        fB[q * N + c] = enc<BF>(ct, fmaf(omega, E.template feq<q>() - fq, fq), q, false);            \
+        const float gq = pull_gen<q, BF>(K, t.box, x, y, zc, 1);                                     \
+        gB[q * N + c] = enc<BF>(ct, fmaf(omega, E.template geq<q>(lat) - gq, gq), q, true);          \
+    }
+                        MBG_UNROLL27(MBG_RS16)
+#undef MBG_RS16
+                    }
+                }
+            }
+            prev = cur;
+            prevf = curf;
+            __syncthreads();
+        }
+    }
+}
+
+// streamed values of the uncovered ghost cells of a fine level
+template <bool BF>
+__global__ void k_ghost_stream16(const LowpK* __restrict__ K, const GhostCell* gl, long long n)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const GhostCell gc = gl[e];
+    const LV16& L = K->L;
+    const DevBox& B = L.box[gc.box];
+    const uint8_t tf = flag_at(L, B, gc.x, gc.y, gc.z);
+    const long long gi = B.goff + fab_lin(B, gc.x, gc.y, gc.z);
+#define MBG_GS16(q)                                                                                               \
+    {                                                                                                             \
+        K->fBg[q * L.NG + gi] = enc<BF>(K->ct, pull16_slow<q, BF>(K, gc.box, gc.x, gc.y, gc.z, tf, 0), q, false); \
+        K->gBg[q * L.NG + gi] = enc<BF>(K->ct, pull16_slow<q, BF>(K, gc.box, gc.x, gc.y, gc.z, tf, 1), q, true);  \
+    }
+    MBG_UNROLL27(MBG_GS16)
+#undef MBG_GS16
+}
+
+// explosion (conservative linear interpolation, as in mbg_fp64.cu) in FP32
+template <bool BF>
+__device__ __forceinline__ float crse16(const LowpK* __restrict__ KC, const int p0[3], int d, int s_, int q,
+                                        bool g)
+{
+    int p[3] = {p0[0], p0[1], p0[2]};
+    p[d] += s_;
+    const LV16& C = KC->L;
+    wrap_pos(C, p);
+    const int o = owner_of(C, p);
+    if (o < 0) return 0.0f;
+    const DevBox& O = C.box[o];
+    const u16* v = g ? KC->s.g : KC->s.f;
+    return dec<BF>(KC->ct, v[q * C.N + O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2])], q, g);
+}
+
+template <bool BF>
+__global__ void k_explode16(const LowpK* __restrict__ KF, const LowpK* __restrict__ KC, const GhostCell* gl,
+                            long long n, u16* fg, u16* gg)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const LV16& F = KF->L;
+    const GhostCell g = gl[e];
+    const DevBox& B = F.box[g.box];
+    int fp[3] = {B.lo[0] + g.x, B.lo[1] + g.y, B.lo[2] + g.z};
+    wrap_pos(F, fp);
+    const int cp[3] = {fp[0] >> 1, fp[1] >> 1, fp[2] >> 1};
+    const float off[3] = {((fp[0] - 2 * cp[0]) + 0.5f) / 2.0f - 0.5f, ((fp[1] - 2 * cp[1]) + 0.5f) / 2.0f - 0.5f,
+                          ((fp[2] - 2 * cp[2]) + 0.5f) / 2.0f - 0.5f};
+    const long long gi = B.goff + fab_lin(B, g.x, g.y, g.z);
+    for (int lat = 0; lat < 2; ++lat) {
+        const bool isg = lat == 1;
+        u16* out = isg ? gg : fg;
+        float alpha[3] = {1.f, 1.f, 1.f};
+        for (int d = 0; d < 3; ++d)
+            for (int q = 0; q < NQ; ++q) {
+                const float u0 = crse16<BF>(KC, cp, d, 0, q, isg);
+                const float up = crse16<BF>(KC, cp, d, 1, q, isg);
+                const float um = crse16<BF>(KC, cp, d, -1, q, isg);
+                const float cen = 0.5f * (up - um);
+                const float forw = 2.0f * (up - u0);
+                const float back = 2.0f * (u0 - um);
+                const float slp = (forw * back >= 0.f) ? fminf(fabsf(forw), fabsf(back)) : 0.f;
+                if (cen != 0.f) alpha[d] = fminf(alpha[d], fminf(slp, fabsf(cen)) / fabsf(cen));
+            }
+        for (int q = 0; q < NQ; ++q) {
+            const float u0 = crse16<BF>(KC, cp, 0, 0, q, isg);
+            const float cx = 0.5f * (crse16<BF>(KC, cp, 0, 1, q, isg) - crse16<BF>(KC, cp, 0, -1, q, isg));
+            const float cy = 0.5f * (crse16<BF>(KC, cp, 1, 1, q, isg) - crse16<BF>(KC, cp, 1, -1, q, isg));
+            const float cz = 0.5f * (crse16<BF>(KC, cp, 2, 1, q, isg) - crse16<BF>(KC, cp, 2, -1, q, isg));
+            out[q * F.NG + gi] = enc<BF>(
+                KF->ct, u0 + off[0] * (alpha[0] * cx) + off[1] * (alpha[1] * cy) + off[2] * (alpha[2] * cz), q, isg);
+        }
+    }
+}
+
+// coalescence: FP64 masked average of the 8 fine children into the override
+// buffer (advance) or the coarse state (initial average_down)
+template <bool BF>
+__global__ void k_coalesce16(const LowpK* __restrict__ KC, const LowpK* __restrict__ KF, const CoalesceCell* cl,
+                             long long n, u16* fo, u16* go, int into_state)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const LV16& C = KC->L;
+    const LV16& F = KF->L;
+    const CoalesceCell cc = cl[e];
+    const DevBox& O = C.box[cc.cbox];
+    const DevBox& A = F.box[cc.fbox];
+    const long long cell = O.voff + val_lin(O, cc.cx, cc.cy, cc.cz);
+    const uint8_t tf = flag_at(C, O, cc.cx, cc.cy, cc.cz);
+    const double small_num = 2.220446049250313e-16 * 1e10;
+    for (int lat = 0; lat < 2; ++lat) {
+        const bool isg = lat == 1;
+        const u16* v = isg ? KF->s.g : KF->s.f;
+        const u16* vg = isg ? KF->s.gg : KF->s.fg;
+        u16* out = isg ? go : fo;
+        const u16* cA = isg ? KC->s.g : KC->s.f;
+#define MBG_CO16(q)                                                                                          \
+        {                                                                                                    \
+            double sum = 0.0, vol = 0.0;                                                                     \
+            for (int kr = 0; kr < 2; ++kr)                                                                   \
+                for (int jr = 0; jr < 2; ++jr)                                                               \
+                    for (int ir = 0; ir < 2; ++ir) {                                                         \
+                        const double fv =                                                                    \
+                            dec<BF>(KF->ct, fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg), q, isg); \
+                        if (fabs(fv - (-1.0)) > small_num) { sum += fv; vol += 1.0; }                        \
+                    }                                                                                        \
+            u16 r;                                                                                           \
+            if (vol > 0.0) r = enc<BF>(KC->ct, (float)(sum / vol), q, isg);                                  \
+            else if (into_state) r = cA[q * C.N + cell];                                                     \
+            else r = enc<BF>(KC->ct, pull16_slow<q, BF>(KC, cc.cbox, cc.cx, cc.cy, cc.cz, tf, isg ? 1 : 0), q, isg); \
+            out[q * C.N + cell] = r;                                                                         \
+        }
+        MBG_UNROLL27(MBG_CO16)
+#undef MBG_CO16
+    }
+}
+
+// FP64 staging ([q][valid cell] in host cell order) <-> 16-bit padded state;
+// one thread per valid cell of a tile
+template <bool BF>
+__global__ void k_encode16(const LowpK* __restrict__ K, const Tile* __restrict__ tiles, const double* __restrict__ src,
+                           long long NV, u16* __restrict__ dst, int isg)
+{
+    const LV16& L = K->L;
+    const Tile t = tiles[blockIdx.x];
+    const DevBox& B = L.box[t.box];
+    const long long c = (long long)t.start + threadIdx.x;
+    const long long vol = (long long)B.n[0] * B.n[1] * B.n[2];
+    if (c >= vol) return;
+    const int x = (int)(c % B.n[0]), y = (int)((c / B.n[0]) % B.n[1]), z = (int)(c / ((long long)B.n[0] * B.n[1]));
+    const long long pc = B.voff + val_lin(B, x, y, z), hc = B.hoff + c;
+    for (int q = 0; q < NQ; ++q) dst[q * L.N + pc] = enc<BF>(K->ct, (float)src[q * NV + hc], q, isg != 0);
+}
+template <bool BF>
+__global__ void k_decode16(const LowpK* __restrict__ K, const Tile* __restrict__ tiles, const u16* __restrict__ src,
+                           long long NV, double* __restrict__ dst, int isg)
+{
+    const LV16& L = K->L;
+    const Tile t = tiles[blockIdx.x];
+    const DevBox& B = L.box[t.box];
+    const long long c = (long long)t.start + threadIdx.x;
+    const long long vol = (long long)B.n[0] * B.n[1] * B.n[2];
+    if (c >= vol) return;
+    const int x = (int)(c % B.n[0]), y = (int)((c / B.n[0]) % B.n[1]), z = (int)(c / ((long long)B.n[0] * B.n[1]));
+    const long long pc = B.voff + val_lin(B, x, y, z), hc = B.hoff + c;
+    for (int q = 0; q < NQ; ++q) dst[q * NV + hc] = (double)dec<BF>(K->ct, src[q * L.N + pc], q, isg != 0);
+}
+
+// macro fields (host layout [box][19][cell]) in FP64 from the decoded state
+template <bool BF>
+__global__ void k_macro16(const LowpK* __restrict__ K, const CodecTab ct, const Tile* tiles, double* out19)
+{
+    const LV16& L = K->L;
+    const Tile t = tiles[blockIdx.x];
+    const DevBox& B = L.box[t.box];
+    const long long c = (long long)t.start + threadIdx.x;
+    const long long vol = (long long)B.n[0] * B.n[1] * B.n[2];
+    if (c >= vol) return;
+    const int x = (int)(c % B.n[0]), y = (int)((c / B.n[0]) % B.n[1]), z = (int)(c / ((long long)B.n[0] * B.n[1]));
+    const uint8_t tf = flag_at(L, B, x, y, z);
+    double* o = out19 + B.hoff * 19 + c;
+    if (!(tf & FL_FLUID)) {
+        for (int k = 0; k < 19; ++k) o[k * vol] = 0.0;
+        return;
+    }
+    const long long cell = B.voff + val_lin(B, x, y, z);
+    const u16* f = K->s.f;
+    const u16* g = K->s.g;
+    MomentAcc<double> acc;
+#define MBG_MA16(q) \
+    acc.template add<q>((double)dec<BF>(ct, f[q * L.N + cell], q, false), (double)dec<BF>(ct, g[q * L.N + cell], q, true));
+    MBG_UNROLL27(MBG_MA16)
+#undef MBG_MA16
+    const Macro<double> m = acc.finish((double)K->ph.mesh_speed, (double)K->ph.Rg, (double)K->ph.cv);
+    const double vals[19] = {m.rho, m.u, m.v, m.w, sqrt(m.u * m.u + m.v * m.v + m.w * m.w), m.two_rho_e,
+                             m.qcx, m.qcy, m.qcz, m.pxx, m.pyy, m.pzz, m.pxy, m.pxz, m.pyz,
+                             m.qx, m.qy, m.qz, m.temp};
+    for (int k = 0; k < 19; ++k) o[k * vol] = vals[k];
+}
+
+// ---- launchers ---------------------------------------------------------------
+template <bool BF>
+void Lowp16<BF>::halo(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s)
+{
+    if (n > 0) k_halo16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, h, n);
+}
+template <bool BF>
+void Lowp16<BF>::halo_periodic(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s)
+{
+    if (n > 0) k_halo_periodic16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, h, n);
+}
+template <bool BF>
+void Lowp16<BF>::fused(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const FusedTile* t, int ntiles,
+                       int grid, cudaStream_t s)
+{
+    if (ntiles > 0) k_fused<BF><<<grid, FT_THREADS, 0, s>>>(k, ct, lat, t, ntiles);
+}
+template <bool BF>
+void Lowp16<BF>::ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s)
+{
+    if (n > 0) k_ghost_stream16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, gl, n);
+}
+template <bool BF>
+void Lowp16<BF>::explode(const LowpK* kf, const LowpK* kc, const GhostCell* gl, long long n, u16* fg, u16* gg,
+                         cudaStream_t s)
+{
+    if (n > 0) k_explode16<BF><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(kf, kc, gl, n, fg, gg);
+}
+template <bool BF>
+void Lowp16<BF>::coalesce(const LowpK* kc, const LowpK* kf, const CoalesceCell* cl, long long n, u16* fo, u16* go,
+                          int into_state, cudaStream_t s)
+{
+    if (n > 0) k_coalesce16<BF><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(kc, kf, cl, n, fo, go, into_state);
+}
+template <bool BF>
+void Lowp16<BF>::encode(const LowpK* k, const Tile* tiles, int ntiles, const double* src, long long NV, u16* dst,
+                        int isg, cudaStream_t s)
+{
+    if (ntiles > 0) k_encode16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, tiles, src, NV, dst, isg);
+}
+template <bool BF>
+void Lowp16<BF>::decode(const LowpK* k, const Tile* tiles, int ntiles, const u16* src, long long NV, double* dst,
+                        int isg, cudaStream_t s)
+{
+    if (ntiles > 0) k_decode16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, tiles, src, NV, dst, isg);
+}
+template <bool BF>
+void Lowp16<BF>::macro(const LowpK* k, const CodecTab& ct, const Tile* tiles, int ntiles, double* out19,
+                       cudaStream_t s)
+{
+    if (ntiles > 0) k_macro16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, tiles, out19);
+}
+
+}  // namespace mbg

@@ -1,0 +1,75 @@
+// mbg_lowp_types.cuh -- types shared by the host code of the 16-bit form
+// (mbg_lowp.cu) and its kernels (mbg_lowp_kern.cuh, compiled once per storage
+// format in mbg_lowp_f16.cu and mbg_lowp_bf16.cu).
+#pragma once
+
+#include "mbg_lowp.h"
+
+namespace mbg {
+
+using u16 = uint16_t;
+using LV16 = LevelView<u16>;
+
+constexpr u16 SENT16 = 0xFFFFu;
+constexpr int FT_THREADS = 256;   // threads of a fused-step CTA
+constexpr int FT_QX = 320;        // shared Q_corr rows: max over tw of th * (tw + 2)
+constexpr int FT_QY = 320;        // max over tw of (th + 2) * tw
+
+struct CodecTab {
+    float frest[NQ], grest[NQ], fsc[NQ], gsc[NQ], fisc[NQ], gisc[NQ];
+};
+
+struct Bufs16 {
+    const u16 *f, *g, *fg, *gg;   // source state (valid, ghost)
+    const u16 *fo, *go;           // coalescence override (coarse levels), or null
+};
+
+// everything the kernels of one level read, for one buffer parity
+struct LowpK {
+    LV16 L;
+    BCParams P;
+    Phys32 ph;
+    CodecTab ct;
+    Lattice<double> lat64;
+    Bufs16 s;                      // source: the current state
+    u16 *fA, *gA;                  // the source again, writable (its pad is filled in place)
+    u16 *fB, *gB, *fBg, *gBg;      // destination: the other buffer
+    const Phys32* phys;            // per-box parameters (batched domains), or null: ph for all boxes
+};
+
+// one cell of a box's pad: box-local coordinates, each -1 .. n
+struct HaloCell {
+    int box;
+    short x, y, z, pad;
+};
+
+struct FusedTile {
+    int box;
+    short x0, y0, z0, z1;
+    short lgw;   // log2 of the tile width in x (3, 4 or 5)
+    short pad;
+};
+
+// kernel launchers, instantiated for FP16 (BF = false) and BF16 (BF = true)
+template <bool BF>
+struct Lowp16 {
+    static void halo(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s);
+    static void halo_periodic(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s);
+    static void fused(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const FusedTile* t, int ntiles,
+                      int grid, cudaStream_t s);
+    static void ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s);
+    static void explode(const LowpK* kf, const LowpK* kc, const GhostCell* gl, long long n, u16* fg, u16* gg,
+                        cudaStream_t s);
+    static void coalesce(const LowpK* kc, const LowpK* kf, const CoalesceCell* cl, long long n, u16* fo, u16* go,
+                         int into_state, cudaStream_t s);
+    static void encode(const LowpK* k, const Tile* tiles, int ntiles, const double* src, long long NV, u16* dst,
+                       int isg, cudaStream_t s);
+    static void decode(const LowpK* k, const Tile* tiles, int ntiles, const u16* src, long long NV, double* dst,
+                       int isg, cudaStream_t s);
+    static void macro(const LowpK* k, const CodecTab& ct, const Tile* tiles, int ntiles, double* out19,
+                      cudaStream_t s);
+};
+extern template struct Lowp16<false>;
+extern template struct Lowp16<true>;
+
+}  // namespace mbg

@@ -11,9 +11,23 @@ import cases
 
 pytestmark = pytest.mark.gpu
 
-# tolerances per form after the stated steps (FP16 keeps 11 significant bits
-# of the deviation from the rest state, BF16 8)
-TOL = {1: {"rho": 1e-4, "u": 1e-2, "T": 1e-4}, 2: {"rho": 1e-3, "u": 8e-2, "T": 1e-3}}
+# Tolerances per form after the stated steps.  FP16 keeps 11 significant bits
+# of each population's deviation from the rest state, BF16 8; the per-step
+# rounding of the stored deviation (up to ~0.2 of the rest value next to a
+# sphere) accumulates over the steps, so rho carries ~1e-4 after 40 steps in
+# FP16.  u is relative to the flow's largest velocity: 1e-3 for flows with a
+# mean velocity (Taylor-Green, inflow), looser for the acoustic pulse, whose
+# |u| ~ 1e-3 is only ~100 FP16 quanta of the deviation.
+TOL = {1: {"rho": 2.5e-4, "u": 1e-3, "T": 1e-3}, 2: {"rho": 2e-3, "u": 1e-2, "T": 2e-3}}
+TOL_PULSE_U = {1: 2e-2, 2: 1.5e-1}
+
+
+def _check(e, prec, u_tol=None):
+    print("16-bit form", prec, "errors", e)
+    tol = dict(TOL[prec])
+    if u_tol is not None:
+        tol["u"] = u_tol
+    assert all(e[k] <= tol[k] for k in e), (e, tol)
 
 
 def _pair(p, levels, prec):
@@ -57,8 +71,7 @@ def test_taylor_green(prec):
     c64, c16 = _pair(p, levels, prec)
     c64.step(50)
     c16.step(50)
-    e = _errors(c64, c16, levels)
-    assert all(e[k] <= TOL[prec][k] for k in e), e
+    _check(_errors(c64, c16, levels), prec)
 
 
 @pytest.mark.parametrize("prec", [1, 2])
@@ -67,8 +80,7 @@ def test_sphere_inflow_outflow(prec):
     c64, c16 = _pair(p, levels, prec)
     c64.step(40)
     c16.step(40)
-    e = _errors(c64, c16, levels)
-    assert all(e[k] <= TOL[prec][k] for k in e), e
+    _check(_errors(c64, c16, levels), prec)
 
 
 @pytest.mark.parametrize("prec", [1, 2])
@@ -77,8 +89,7 @@ def test_two_level_pulse(prec):
     c64, c16 = _pair(p, levels, prec)
     c64.step(20)
     c16.step(20)
-    e = _errors(c64, c16, levels)
-    assert all(e[k] <= TOL[prec][k] for k in e), e
+    _check(_errors(c64, c16, levels), prec, TOL_PULSE_U[prec])
 
 
 def test_three_level_sphere_fp16():
@@ -86,8 +97,7 @@ def test_three_level_sphere_fp16():
     c64, c16 = _pair(p, levels, 1)
     c64.step(5)
     c16.step(5)
-    e = _errors(c64, c16, levels)
-    assert all(e[k] <= TOL[1][k] for k in e), e
+    _check(_errors(c64, c16, levels), 1)
 
 
 @pytest.mark.parametrize("prec", [1, 2])
