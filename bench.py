@@ -132,6 +132,11 @@ def run_form(form, steps, warmup, device_index):
         host.append((f, g))
     for _ in range(warmup):
         ctx.step(1)
+    tuning = None
+    if form != "fp64":
+        # the library's autotuner picks each level's step variant on this data
+        ctx.autotune(3)
+        tuning = [ctx.tuning(lev) for lev in range(nlev)]
     ctx.synchronize()
     ctx.set_timing(True)
     n0 = ctx.launch_count()
@@ -150,7 +155,7 @@ def run_form(form, steps, warmup, device_index):
     res = {"form": form, "ms_per_step": ms / steps, "mlups": cups * steps / (ms * 1e-3) / 1e6,
            "cell_updates_per_step": cups, "gpu_launches": launches,
            "kernels": {k: {"launches": n, "ms": t} for k, (n, t) in timing.items() if n},
-           "clocks": clk.summary()}
+           "clocks": clk.summary(), "tuning": tuning}
     # end to end through the C ABI with pinned host buffers: upload of the
     # initial state, K steps each followed by the EB-force read-back (the
     # reference computes it every step), download of the state

@@ -171,6 +171,56 @@ mbg_status mbg_set_timing(mbg_ctx* ctx, int enable);
 int mbg_timing_count(void);
 mbg_status mbg_timing(mbg_ctx* ctx, int k, const char** name, long long* launches, double* ms);
 
+/* ---- autotuner ----------------------------------------------------------------
+ * No counterpart in the reference.  The 16-bit forms have several
+ * implementations of the level step: variant 0 runs it in two passes (Q_corr,
+ * then collision), variants 1-3 fuse it into one pass over runs of 4, 8 or 16
+ * planes per thread block.  mbg_autotune times every variant `reps` times on
+ * each level's current data and keeps the fastest per level; the state is not
+ * changed.  mbg_tuning reports a level's chosen variant and the mean time per
+ * step of each variant in ms (0 where not timed).  FP64 contexts have one
+ * variant; both calls succeed and report variant 0. */
+mbg_status mbg_autotune(mbg_ctx* ctx, int reps);
+mbg_status mbg_tuning(mbg_ctx* ctx, int lev, int* variant, double ms[4]);
+
+/* ---- batched independent domains -----------------------------------------
+ * No counterpart in the reference, which runs one domain per process.  Many
+ * small periodic domains advance together, each with its own cell counts,
+ * physical extent (the q-correction gradient uses its per-axis 1/dx),
+ * viscosity and diffusivity; the gradient is one-sided at each domain's faces
+ * as at the domain box of a single run.  Every launch covers all domains: a
+ * pad fill and the step, the fused variants as a persistent grid walking a
+ * device work list of column tiles (largest domains first).  Steps are
+ * replayed from a CUDA graph of two steps captured on first use;
+ * mbg_batch_autotune times the step variants on the live data (state
+ * unchanged) and keeps the fastest.  16-bit forms only (common->precision
+ * MBG_FP32C_F16S or MBG_FP32C_BF16S); the other common fields (dx_outer,
+ * dt_outer, adiabatic_exponent, m_bar and the storage's reference state
+ * rho_ref, t_ref, u_ref) apply to every domain.  Host state layout:
+ * [domain][q][cell], cells x-fastest, domains in the order given; macro
+ * fields [domain][19][cell] as mbg_get_macro.  A failed creation leaves its
+ * message in mbg_last_error(NULL). */
+typedef struct mbg_batch mbg_batch;
+typedef struct mbg_domain {
+    int n_cell[3];
+    double prob_lo[3], prob_hi[3];
+    double nu, alpha;
+} mbg_domain;
+mbg_status mbg_batch_create(const mbg_params* common, int ndom, const mbg_domain* doms, void* cuda_stream,
+                            mbg_batch** out);
+mbg_status mbg_batch_cells(const mbg_batch* b, long long* ncells);
+mbg_status mbg_batch_set_state(mbg_batch* b, const double* f, const double* g);
+mbg_status mbg_batch_get_state(mbg_batch* b, double* f, double* g);
+mbg_status mbg_batch_get_macro(mbg_batch* b, double* out19);
+mbg_status mbg_batch_step(mbg_batch* b, int nsteps);
+mbg_status mbg_batch_autotune(mbg_batch* b, int reps);
+mbg_status mbg_batch_tuning(mbg_batch* b, int* variant, double ms[4]);
+mbg_status mbg_batch_synchronize(mbg_batch* b);
+long long mbg_batch_launch_count(const mbg_batch* b);
+void* mbg_batch_stream(const mbg_batch* b);
+const char* mbg_batch_last_error(const mbg_batch* b);
+void mbg_batch_destroy(mbg_batch* b);
+
 /* ---- step without device allocation --------------------------------------
  * No counterpart in the reference.  For callers that cannot let a library
  * allocate device memory: a host code that has given the GPU to its own

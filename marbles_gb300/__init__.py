@@ -55,6 +55,12 @@ class MbgParams(C.Structure):
     ]
 
 
+class MbgDomain(C.Structure):
+    """mirror of mbg_domain (one domain of a batch)"""
+    _fields_ = [("n_cell", C.c_int * 3), ("prob_lo", C.c_double * 3), ("prob_hi", C.c_double * 3),
+                ("nu", C.c_double), ("alpha", C.c_double)]
+
+
 _lib = None
 
 
@@ -80,6 +86,25 @@ def lib():
         L.mbg_advance_level.argtypes = [vp, C.c_int]
         L.mbg_fillpatch.argtypes = [vp, C.c_int]
         L.mbg_average_down.argtypes = [vp, C.c_int, C.c_int]
+        L.mbg_autotune.argtypes = [vp, C.c_int]
+        L.mbg_batch_create.argtypes = [C.POINTER(MbgParams), C.c_int, C.POINTER(MbgDomain), vp, C.POINTER(vp)]
+        L.mbg_batch_cells.argtypes = [vp, C.POINTER(C.c_longlong)]
+        L.mbg_batch_set_state.argtypes = [vp, dp, dp]
+        L.mbg_batch_get_state.argtypes = [vp, dp, dp]
+        L.mbg_batch_get_macro.argtypes = [vp, dp]
+        L.mbg_batch_step.argtypes = [vp, C.c_int]
+        L.mbg_batch_autotune.argtypes = [vp, C.c_int]
+        L.mbg_batch_tuning.argtypes = [vp, C.POINTER(C.c_int), dp]
+        L.mbg_batch_synchronize.argtypes = [vp]
+        L.mbg_batch_launch_count.argtypes = [vp]
+        L.mbg_batch_launch_count.restype = C.c_longlong
+        L.mbg_batch_stream.argtypes = [vp]
+        L.mbg_batch_stream.restype = vp
+        L.mbg_batch_last_error.argtypes = [vp]
+        L.mbg_batch_last_error.restype = C.c_char_p
+        L.mbg_batch_destroy.argtypes = [vp]
+        L.mbg_batch_destroy.restype = None
+        L.mbg_tuning.argtypes = [vp, C.c_int, C.POINTER(C.c_int), dp]
         L.mbg_eb_forces.argtypes = [vp, dp]
         L.mbg_synchronize.argtypes = [vp]
         L.mbg_launch_count.argtypes = [vp]
@@ -203,6 +228,17 @@ class Context:
     def average_down(self, crse_lev, ng):
         self._check(self.L.mbg_average_down(self.h, crse_lev, ng), "mbg_average_down")
 
+    def autotune(self, reps=3):
+        """Time the step variants of every level and keep the fastest (16-bit forms)."""
+        self._check(self.L.mbg_autotune(self.h, reps), "mbg_autotune")
+
+    def tuning(self, lev):
+        """(chosen variant, [ms per step of variants 0..3]) of level lev."""
+        v = C.c_int()
+        ms = np.zeros(4)
+        self._check(self.L.mbg_tuning(self.h, lev, C.byref(v), _dp(ms)), "mbg_tuning")
+        return v.value, ms.tolist()
+
     def eb_forces(self):
         out = np.zeros(3)
         self._check(self.L.mbg_eb_forces(self.h, _dp(out)), "mbg_eb_forces")
@@ -232,6 +268,85 @@ class Context:
     def close(self):
         if getattr(self, "h", None):
             self.L.mbg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent periodic domains stepped together (mbg_batch_*).
+
+    domains: sequence of (n_cell[3], prob_lo[3], prob_hi[3], nu, alpha)."""
+
+    def __init__(self, common, domains, stream=None):
+        self.L = lib()
+        arr = (MbgDomain * len(domains))()
+        for i, (n, lo, hi, nu, alpha) in enumerate(domains):
+            arr[i].n_cell[:] = [int(v) for v in n]
+            arr[i].prob_lo[:] = [float(v) for v in lo]
+            arr[i].prob_hi[:] = [float(v) for v in hi]
+            arr[i].nu, arr[i].alpha = float(nu), float(alpha)
+        h = C.c_void_p()
+        st = self.L.mbg_batch_create(C.byref(common), len(domains), arr, stream, C.byref(h))
+        if st != 0:
+            raise MbgError("mbg_batch_create: %s: %s" % (STATUS.get(st, st), self.L.mbg_last_error(None).decode()))
+        self.h = h
+        n = C.c_longlong()
+        self._check(self.L.mbg_batch_cells(self.h, C.byref(n)), "mbg_batch_cells")
+        self.n = n.value
+
+    def _check(self, st, what):
+        if st != 0:
+            raise MbgError("%s: %s: %s" % (what, STATUS.get(st, st), self.L.mbg_batch_last_error(self.h).decode()))
+
+    def ncells(self):
+        return self.n
+
+    def set_state(self, f, g):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        assert f.size == g.size == self.n * NQ
+        self._check(self.L.mbg_batch_set_state(self.h, _dp(f), _dp(g)), "mbg_batch_set_state")
+
+    def get_state(self):
+        f = np.empty(self.n * NQ)
+        g = np.empty(self.n * NQ)
+        self._check(self.L.mbg_batch_get_state(self.h, _dp(f), _dp(g)), "mbg_batch_get_state")
+        return f, g
+
+    def get_macro(self):
+        out = np.empty(self.n * 19)
+        self._check(self.L.mbg_batch_get_macro(self.h, _dp(out)), "mbg_batch_get_macro")
+        return out
+
+    def step(self, n=1):
+        self._check(self.L.mbg_batch_step(self.h, n), "mbg_batch_step")
+
+    def autotune(self, reps=3):
+        self._check(self.L.mbg_batch_autotune(self.h, reps), "mbg_batch_autotune")
+
+    def tuning(self):
+        v = C.c_int()
+        ms = np.zeros(4)
+        self._check(self.L.mbg_batch_tuning(self.h, C.byref(v), _dp(ms)), "mbg_batch_tuning")
+        return v.value, ms.tolist()
+
+    def synchronize(self):
+        self._check(self.L.mbg_batch_synchronize(self.h), "mbg_batch_synchronize")
+
+    def launch_count(self):
+        return self.L.mbg_batch_launch_count(self.h)
+
+    def stream(self):
+        return self.L.mbg_batch_stream(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mbg_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -72,7 +72,7 @@ struct Level {
 // kernel classes timed by mbg_set_timing
 enum { TK_MOMENTS = 0, TK_COLLIDE, TK_GHOST_STREAM, TK_GHOST_MOMENTS, TK_EXPLODE, TK_COALESCE, TK_FUSED, TK_HALO, TK_OTHER, TK_N };
 static const char* TK_NAMES[TK_N] = {"k_moments", "k_collide", "k_ghost_stream", "k_ghost_moments",
-                                     "k_explode", "k_coalesce", "k_lowp_fused", "k_halo", "other"};
+                                     "k_explode", "k_coalesce", "k_lowp_step", "k_halo", "other"};
 
 struct mbg_ctx {
     mbg_params p;
@@ -412,7 +412,7 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
         B.foff = foff;
         B.goff = -1;
         B.phys = 0;
-        B.pad = 0;
+        B.own_domain = 0;
         voff += L.boxes[n].vol();
         foff += L.boxes[n].gvol();
     }
@@ -774,6 +774,37 @@ mbg_status mbg_fillpatch(mbg_ctx* ctx, int lev)
     if (lev < 0 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_fillpatch: level not defined");
     if (lev == 0) return MBG_OK;  // level-0 ghosts are never stored: pulls read neighbours and BCs directly
     return explode(ctx, lev);
+}
+
+mbg_status mbg_autotune(mbg_ctx* ctx, int reps)
+{
+    if (!ctx) return MBG_EINVAL;
+    if (reps < 1) return fail(ctx, MBG_EINVAL, "mbg_autotune: reps must be >= 1");
+    if (ctx->p.precision == MBG_FP64) return MBG_OK;
+    const int nl = (int)ctx->lv.size();
+    for (int lev = 0; lev < nl; ++lev) {
+        Level& L = ctx->lv[lev];
+        const bool has_finer = lev + 1 < nl;
+        mbg_status st = lowp_autotune(L.lowp, L.plan, ctx->bc, has_finer ? L.d_coal1 : nullptr,
+                                      has_finer ? L.ncoal1 : 0, has_finer ? &ctx->lv[lev + 1].lowp : nullptr,
+                                      has_finer ? &ctx->lv[lev + 1].plan : nullptr, reps, ctx->s, ctx->err);
+        if (st != MBG_OK) return st;
+    }
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+mbg_status mbg_tuning(mbg_ctx* ctx, int lev, int* variant, double ms[4])
+{
+    if (!ctx || !variant || !ms) return MBG_EINVAL;
+    if (lev < 0 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_EINVAL, "mbg_tuning: no such level");
+    if (ctx->p.precision == MBG_FP64) {
+        *variant = 0;
+        for (int v = 0; v < 4; ++v) ms[v] = 0.0;
+        return MBG_OK;
+    }
+    lowp_variant(ctx->lv[lev].lowp, variant, ms);
+    return MBG_OK;
 }
 
 mbg_status mbg_average_down(mbg_ctx* ctx, int crse_lev, int crse_ng)

@@ -10,17 +10,23 @@ namespace mbg {
 // ---- explosion: conservative linear interpolation of the coarse level ------
 // (AMReX cell_cons_interp as called at Source/FillPatchOps.H:124-128: MC
 // slopes, one limiter factor per direction shared by all 27 components)
-__device__ __forceinline__ double crse_at(const LV& C, const int p0[3], int d, int s, int q, const double* v)
+
+// storage index (without the component offset) of coarse cell p0 + s e_d, or
+// -1 where no coarse box holds it
+__device__ __forceinline__ long long crse_index(const LV& C, const int p0[3], int d, int s)
 {
     int p[3] = {p0[0], p0[1], p0[2]};
     p[d] += s;
     wrap_pos(C, p);
     const int o = owner_of(C, p);
-    if (o < 0) return 0.0;  // plans reject fine levels whose stencil leaves the coarse level
+    if (o < 0) return -1;  // plans reject fine levels whose stencil leaves the coarse level
     const DevBox& O = C.box[o];
-    return v[q * C.N + O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2])];
+    return O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2]);
 }
 
+// One thread per fine ghost cell (neighbouring threads read neighbouring
+// coarse cells, so each component's loads coalesce); the seven coarse cells
+// of the stencil are located once, then every component is read from them.
 __global__ void k_explode(LV F, LV C, const GhostCell* gl, long long n, const double* fc, const double* gc_,
                           double* fg, double* gg)
 {
@@ -34,15 +40,21 @@ __global__ void k_explode(LV F, LV C, const GhostCell* gl, long long n, const do
     const double off[3] = {((fp[0] - 2 * cp[0]) + 0.5) / 2.0 - 0.5, ((fp[1] - 2 * cp[1]) + 0.5) / 2.0 - 0.5,
                            ((fp[2] - 2 * cp[2]) + 0.5) / 2.0 - 0.5};
     const long long gi = B.goff + fab_lin(B, g.x, g.y, g.z);
+    // centre, then -/+ along x, y, z
+    long long ix[7];
+    ix[0] = crse_index(C, cp, 0, 0);
+    for (int d = 0; d < 3; ++d) {
+        ix[1 + 2 * d] = crse_index(C, cp, d, -1);
+        ix[2 + 2 * d] = crse_index(C, cp, d, 1);
+    }
     for (int lat = 0; lat < 2; ++lat) {
         const double* v = lat ? gc_ : fc;
         double* out = lat ? gg : fg;
+        auto at = [&](int k, int q) { return ix[k] >= 0 ? v[q * C.N + ix[k]] : 0.0; };
         double alpha[3] = {1.0, 1.0, 1.0};
         for (int d = 0; d < 3; ++d) {
             for (int q = 0; q < NQ; ++q) {
-                const double u0 = crse_at(C, cp, d, 0, q, v);
-                const double up = crse_at(C, cp, d, 1, q, v);
-                const double um = crse_at(C, cp, d, -1, q, v);
+                const double u0 = at(0, q), um = at(1 + 2 * d, q), up = at(2 + 2 * d, q);
                 const double cen = 0.5 * (up - um);
                 const double forw = 2.0 * (up - u0);
                 const double back = 2.0 * (u0 - um);
@@ -51,56 +63,67 @@ __global__ void k_explode(LV F, LV C, const GhostCell* gl, long long n, const do
             }
         }
         for (int q = 0; q < NQ; ++q) {
-            const double u0 = crse_at(C, cp, 0, 0, q, v);
-            const double cx = 0.5 * (crse_at(C, cp, 0, 1, q, v) - crse_at(C, cp, 0, -1, q, v));
-            const double cy = 0.5 * (crse_at(C, cp, 1, 1, q, v) - crse_at(C, cp, 1, -1, q, v));
-            const double cz = 0.5 * (crse_at(C, cp, 2, 1, q, v) - crse_at(C, cp, 2, -1, q, v));
+            const double u0 = at(0, q);
+            const double cx = 0.5 * (at(2, q) - at(1, q));
+            const double cy = 0.5 * (at(4, q) - at(3, q));
+            const double cz = 0.5 * (at(6, q) - at(5, q));
             out[q * F.NG + gi] = u0 + off[0] * (alpha[0] * cx) + off[1] * (alpha[1] * cy) + off[2] * (alpha[2] * cz);
         }
     }
+}
+
+// streamed value of a runtime direction (the coalescence's fallback where
+// every child is masked)
+__device__ __noinline__ double pull_rt(int q, const LV& C, const BCParams& P, const DevBox& O, int x, int y, int z,
+                                       uint8_t tf, const double* v, const double* vg, bool is_g,
+                                       const Lattice<double>& lat)
+{
+    switch (q) {
+#define MBG_PRT(qq) \
+    case qq: return pull<qq>(C, P, O, x, y, z, tf, false, v, vg, is_g, lat);
+        MBG_UNROLL27(MBG_PRT)
+#undef MBG_PRT
+    }
+    return -1.0;
 }
 
 // ---- coalescence: masked average of the 8 fine children --------------------
 // (masked_avgdown, Source/Utilities.H:315-350).  into_state: write into the
 // coarse state buffer directly (initial average_down, ng = 0); otherwise into
 // the coarse post-stream override buffer, with the coarse streamed value
-// where every child is masked.
+// where every child is masked.  One thread per (coarse cell, direction):
+// blockIdx.y is the direction, so a warp reads one component of 32
+// consecutive coarse cells' children.
 __global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, const CoalesceCell* cl, long long n,
                            const double* ff, const double* gf, const double* ffg, const double* gfg,
                            const double* fcA, const double* gcA, const double* fcAg, const double* gcAg,
                            double* fcB, double* gcB, int into_state)
 {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
     if (e >= n) return;
     const CoalesceCell cc = cl[e];
     const DevBox& O = C.box[cc.cbox];
     const DevBox& A = F.box[cc.fbox];
     const long long cell = O.voff + val_lin(O, cc.cx, cc.cy, cc.cz);
-    const uint8_t tf = flag_at(C, O, cc.cx, cc.cy, cc.cz);
     const double masked = -1.0;
     for (int lat = 0; lat < 2; ++lat) {
         const double* v = lat ? gf : ff;
         const double* vg = lat ? gfg : ffg;
-        double* out = lat ? gcB : fcB;
         const double* cA = lat ? gcA : fcA;
-        const double* cAg = lat ? gcAg : fcAg;
-#define MBG_CO64(q)                                                                               \
-        {                                                                                         \
-            double s = 0.0, vol = 0.0;                                                            \
-            for (int kr = 0; kr < 2; ++kr)                                                        \
-                for (int jr = 0; jr < 2; ++jr)                                                    \
-                    for (int ir = 0; ir < 2; ++ir) {                                              \
-                        const double fv = fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg); \
-                        if (fabs(fv - masked) > ph.small_num) { s += fv; vol += 1.0; }            \
-                    }                                                                             \
-            double r;                                                                             \
-            if (vol > 0.0) r = s / vol;                                                           \
-            else if (into_state) r = cA[q * C.N + cell];                                          \
-            else r = pull<q>(C, P, O, cc.cx, cc.cy, cc.cz, tf, false, cA, cAg, lat == 1, ph.lat); \
-            out[q * C.N + cell] = r;                                                              \
-        }
-        MBG_UNROLL27(MBG_CO64)
-#undef MBG_CO64
+        double s = 0.0, vol = 0.0;
+        for (int kr = 0; kr < 2; ++kr)
+            for (int jr = 0; jr < 2; ++jr)
+                for (int ir = 0; ir < 2; ++ir) {
+                    const double fv = fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg);
+                    if (fabs(fv - masked) > ph.small_num) { s += fv; vol += 1.0; }
+                }
+        double r;
+        if (vol > 0.0) r = s / vol;
+        else if (into_state) r = cA[q * C.N + cell];
+        else r = pull_rt(q, C, P, O, cc.cx, cc.cy, cc.cz, flag_at(C, O, cc.cx, cc.cy, cc.cz), cA,
+                         lat ? gcAg : fcAg, lat == 1, ph.lat);
+        (lat ? gcB : fcB)[q * C.N + cell] = r;
     }
 }
 
@@ -108,7 +131,7 @@ void launch_explode(const LevelPlan& fine, const LevelPlan& crse, const double* 
                     double* gg, cudaStream_t s)
 {
     if (fine.nghost_cells == 0) return;
-    const int th = 64;
+    const int th = 128;
     const long long nb = (fine.nghost_cells + th - 1) / th;
     k_explode<<<(unsigned)nb, th, 0, s>>>(fine.view64, crse.view64, fine.ghost_list, fine.nghost_cells, fc, gc, fg,
                                           gg);
@@ -120,9 +143,9 @@ void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParam
                      const double* gcAg, double* fcB, double* gcB, int into_state, cudaStream_t s)
 {
     if (n == 0) return;
-    const int th = 64;
-    const long long nb = (n + th - 1) / th;
-    k_coalesce<<<(unsigned)nb, th, 0, s>>>(crse.view64, fine.view64, P, ph, list, n, ff, gf, ffg, gfg, fcA, gcA,
+    const int th = 128;
+    const dim3 grid((unsigned)((n + th - 1) / th), NQ);
+    k_coalesce<<<grid, th, 0, s>>>(crse.view64, fine.view64, P, ph, list, n, ff, gf, ffg, gfg, fcA, gcA,
                                            fcAg, gcAg, fcB, gcB, into_state);
 }
 

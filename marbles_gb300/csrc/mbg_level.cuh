@@ -48,7 +48,7 @@ struct DevBox {
     int all_fluid;    // no solid cell anywhere in the grown fab
     int vfluid;       // every cell of the box grown by one is fluid
     int phys;         // index of the box's physical parameters (batched domains)
-    int pad;
+    int own_domain;   // the box is a periodic domain of its own (batched domains)
 };
 
 // boundary conditions of the domain (level 0 only)

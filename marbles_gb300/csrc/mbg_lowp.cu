@@ -24,9 +24,12 @@ struct LowpDev {
     bool with_override = false;
     LowpK* dk = nullptr;         // device copies [2]
     DevBox* box16 = nullptr;     // the level's boxes in the padded layout
-    FusedTile* tiles = nullptr;
-    int ntiles = 0;
-    int grid = 0;                // CTAs of the fused launch
+    // step variants: 0 two-pass, 1.. fused with runs of FUSED_ZC[v - 1] planes
+    FusedTile* ftiles[3] = {nullptr, nullptr, nullptr};
+    int nftiles[3] = {0, 0, 0};
+    int variant = 0;
+    double variant_ms[4] = {0, 0, 0, 0};   // tuner's timings (0: not timed)
+    float* qs = nullptr;         // Q_corr of the two-pass step, [3][N]
     HaloCell* halo = nullptr;    // every pad cell of every box
     long long nhalo = 0;
     u16* fo = nullptr;           // coalescence override buffers
@@ -68,7 +71,7 @@ static mbg_status lalloc(LowpLevel& L, void** p, size_t bytes, std::string& err)
     return MBG_OK;
 }
 
-static Phys32 phys32(const mbg_params& p, double dt, const double idx[3])
+Phys32 phys32(const mbg_params& p, double dt, const double idx[3])
 {
     Phys32 ph;
     ph.mesh_speed = (float)(p.dx_outer / p.dt_outer);
@@ -96,7 +99,7 @@ static Bufs16 bufs(const LowpLevel& L, int b)
 }
 
 // codec of the storage: the equilibria at the reference state and the scales
-static CodecTab make_codec(const mbg_params& p)
+CodecTab make_codec(const mbg_params& p)
 {
     CodecTab ct;
     const Lattice<double> lat64 = make_lattice<double>();
@@ -122,7 +125,7 @@ static CodecTab make_codec(const mbg_params& p)
 }
 
 // padded boxes: strides, storage offsets; returns the padded cell count
-static long long pad_boxes(std::vector<DevBox>& box)
+long long pad_boxes(std::vector<DevBox>& box)
 {
     long long np = 0;
     for (DevBox& B : box) {
@@ -137,7 +140,7 @@ static long long pad_boxes(std::vector<DevBox>& box)
 
 // every pad cell of every box, faces first, then edges, then corners, so that
 // neighbouring threads share the set of directions they fill
-static std::vector<HaloCell> halo_cells(const std::vector<DevBox>& box)
+std::vector<HaloCell> halo_cells(const std::vector<DevBox>& box)
 {
     std::vector<HaloCell> out;
     for (int nz = 1; nz <= 3; ++nz)
@@ -160,9 +163,10 @@ static std::vector<HaloCell> halo_cells(const std::vector<DevBox>& box)
     return out;
 }
 
+
 // fused-step tiles: tile width the smallest of 8, 16, 32 that covers the box
 // (32 for wider boxes), runs of zc planes
-static std::vector<FusedTile> fused_tiles(const std::vector<DevBox>& box, int zc)
+std::vector<FusedTile> fused_tiles(const std::vector<DevBox>& box, int zc)
 {
     std::vector<FusedTile> tiles;
     for (size_t n = 0; n < box.size(); ++n) {
@@ -192,16 +196,17 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     for (size_t n = 0; n < box.size(); ++n) box[n].hoff = hbox[n].voff;
     L.N = pad_boxes(box);
     const std::vector<HaloCell> halo = halo_cells(box);
-    const std::vector<FusedTile> tiles = fused_tiles(box, 8);
-    D->ntiles = (int)tiles.size();
-    D->grid = D->ntiles;
     D->nhalo = (long long)halo.size();
     mbg_status st;
     if ((st = lalloc(L, (void**)&D->box16, box.size() * sizeof(DevBox), err)) != MBG_OK) return st;
-    if ((st = lalloc(L, (void**)&D->tiles, tiles.size() * sizeof(FusedTile), err)) != MBG_OK) return st;
+    for (int v = 0; v < 3; ++v) {
+        const std::vector<FusedTile> tiles = fused_tiles(box, FUSED_ZC[v]);
+        D->nftiles[v] = (int)tiles.size();
+        if ((st = lalloc(L, (void**)&D->ftiles[v], tiles.size() * sizeof(FusedTile), err)) != MBG_OK) return st;
+        cudaMemcpy(D->ftiles[v], tiles.data(), tiles.size() * sizeof(FusedTile), cudaMemcpyHostToDevice);
+    }
     if ((st = lalloc(L, (void**)&D->halo, halo.size() * sizeof(HaloCell), err)) != MBG_OK) return st;
     cudaMemcpy(D->box16, box.data(), box.size() * sizeof(DevBox), cudaMemcpyHostToDevice);
-    cudaMemcpy(D->tiles, tiles.data(), tiles.size() * sizeof(FusedTile), cudaMemcpyHostToDevice);
     cudaMemcpy(D->halo, halo.data(), halo.size() * sizeof(HaloCell), cudaMemcpyHostToDevice);
     const size_t sb = (size_t)L.N * NQ * 2;
     for (int b = 0; b < 2; ++b) {
@@ -220,6 +225,8 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     if ((st = lalloc(L, (void**)&D->go, sb, err)) != MBG_OK) return st;
     cudaMemset(D->fo, 0xFF, sb);
     cudaMemset(D->go, 0xFF, sb);
+    if ((st = lalloc(L, (void**)&D->qs, (size_t)L.N * 3 * sizeof(float), err)) != MBG_OK) return st;
+    cudaMemset(D->qs, 0, (size_t)L.N * 3 * sizeof(float));
     if ((st = lalloc(L, (void**)&L.tmp, (size_t)N * NQ * sizeof(double), err)) != MBG_OK) return st;
     if ((st = lalloc(L, (void**)&D->dk, 2 * sizeof(LowpK), err)) != MBG_OK) return st;
     cudaError_t e = cudaDeviceSynchronize();
@@ -364,13 +371,78 @@ int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const Le
         run(LOWP_STAGE_GHOST_STREAM, [&] { LOWP16(bf, ghost_stream, k, plan.ghost_list, plan.nghost_cells, s); });
         ++launches;
     }
-    run(LOWP_STAGE_FUSED, [&] { LOWP16(bf, fused, k, D->ct, D->lat, D->tiles, D->ntiles, D->grid, s); });
-    ++launches;
+    if (D->variant == 0) {
+        run(LOWP_STAGE_FUSED,
+            [&] { LOWP16(bf, two_pass, k, D->ct, D->lat, plan.tiles, plan.ntiles, D->halo, D->nhalo, D->qs, s); });
+        launches += 3;
+    } else {
+        const int v = D->variant - 1;
+        run(LOWP_STAGE_FUSED,
+            [&] { LOWP16(bf, fused, k, D->ct, D->lat, D->ftiles[v], D->nftiles[v], D->nftiles[v], s); });
+        ++launches;
+    }
     L.cur = 1 - A;
     (void)p;
     (void)dt;
     (void)idx;
     return launches;
+}
+
+int lowp_variants() { return 4; }
+
+// Time every step variant on the level's current data and keep the fastest.
+// The trials recompute the same step from the same source buffer (the
+// parity is not flipped), so the state is unchanged.
+mbg_status lowp_autotune(LowpLevel& L, const LevelPlan& plan, const BCParams& bc, const CoalesceCell* coal,
+                         long long ncoal, const LowpLevel* fine, const LevelPlan* fplan, int reps, cudaStream_t s,
+                         std::string& err)
+{
+    LowpDev* D = dev_of(L);
+    const int keep = L.cur;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const LowpRunner run = [](int, const std::function<void()>& launch) { launch(); };
+    mbg_params dummy{};
+    const double idx0[3] = {0, 0, 0};
+    double best = 0;
+    int best_v = 0;
+    for (int v = 0; v < lowp_variants(); ++v) {
+        D->variant = v;
+        lowp_advance(dummy, bc, L, plan, 0.0, idx0, coal, ncoal, fine, fplan, s, run);   // warm-up
+        L.cur = keep;
+        cudaEventRecord(a, s);
+        for (int r = 0; r < reps; ++r) {
+            lowp_advance(dummy, bc, L, plan, 0.0, idx0, coal, ncoal, fine, fplan, s, run);
+            L.cur = keep;
+        }
+        cudaEventRecord(b, s);
+        cudaError_t e = cudaEventSynchronize(b);
+        if (e != cudaSuccess) {
+            err = std::string("autotune: ") + cudaGetErrorString(e);
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            return MBG_ECUDA;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        D->variant_ms[v] = ms / reps;
+        if (v == 0 || D->variant_ms[v] < best) {
+            best = D->variant_ms[v];
+            best_v = v;
+        }
+    }
+    D->variant = best_v;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return MBG_OK;
+}
+
+void lowp_variant(LowpLevel& L, int* variant, double ms[4])
+{
+    LowpDev* D = dev_of(L);
+    *variant = D->variant;
+    for (int v = 0; v < 4; ++v) ms[v] = D->variant_ms[v];
 }
 
 void lowp_explode(LowpLevel& F, const LevelPlan& fplan, const LowpLevel& C, const LevelPlan& cplan, cudaStream_t s)

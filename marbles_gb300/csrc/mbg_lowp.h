@@ -42,6 +42,13 @@ using LowpRunner = std::function<void(int stage, const std::function<void()>& la
 int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const LevelPlan& plan, double dt,
                  const double idx[3], const CoalesceCell* coal, long long ncoal, const LowpLevel* fine,
                  const LevelPlan* fplan, cudaStream_t s, const LowpRunner& run);
+// step variants (0: two-pass, 1..3: fused with 4, 8, 16-plane runs) and the
+// tuner that times them on the level's data and keeps the fastest
+int lowp_variants();
+mbg_status lowp_autotune(LowpLevel& L, const LevelPlan& plan, const BCParams& bc, const CoalesceCell* coal,
+                         long long ncoal, const LowpLevel* fine, const LevelPlan* fplan, int reps, cudaStream_t s,
+                         std::string& err);
+void lowp_variant(LowpLevel& L, int* variant, double ms[4]);
 void lowp_explode(LowpLevel& F, const LevelPlan& fplan, const LowpLevel& C, const LevelPlan& cplan, cudaStream_t s);
 void lowp_average_down(LowpLevel& C, const LevelPlan& cplan, const LowpLevel& F, const LevelPlan& fplan,
                        const CoalesceCell* list, long long n, cudaStream_t s);

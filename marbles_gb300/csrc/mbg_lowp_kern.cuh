@@ -300,6 +300,7 @@ __device__ __forceinline__ bool present(const LV16& L, const DevBox& B, int x, i
     p[d] += s;
     const int gd = B.lo[d] + p[d];
     if (gd < L.dlo[d] || gd > L.dhi[d]) return false;
+    if (B.own_domain && (p[d] < 0 || p[d] >= B.n[d])) return false;
     return flag_at(L, B, p[0], p[1], p[2]) & FL_FLUID;
 }
 
@@ -467,6 +468,170 @@ __global__ void __launch_bounds__(FT_THREADS, 2)
     }
 }
 
+// ---- two-pass step ------------------------------------------------------------
+// pass 1 (k_qcorr16): Q_corr of every valid cell into qs[d * N + c], padded
+// layout; k_qhalo16 then fills the face cells of each box's pad with Q_corr
+// as the owning box (or, on the coarse-fine shell, the box itself) computes
+// it; pass 2 (k_collide16) pulls again, takes the gradient from qs and
+// collides.  No barriers and no halo recomputation; the populations are read
+// twice.
+
+// box-local cell of thread threadIdx.x of a Tile (128 cells in x-fastest order)
+__device__ __forceinline__ bool tile_cell(const DevBox& B, const Tile& t, int& x, int& y, int& z)
+{
+    const long long ci = (long long)t.start + threadIdx.x;
+    const long long nxy = (long long)B.n[0] * B.n[1];
+    if (ci >= nxy * B.n[2]) return false;
+    z = (int)(ci / nxy);
+    const int r = (int)(ci - (long long)z * nxy);
+    y = r / B.n[0];
+    x = r - y * B.n[0];
+    return true;
+}
+
+template <bool BF>
+__device__ __forceinline__ MomentAcc<float> moments_at(const LowpK* __restrict__ K, const CodecTab& ct,
+                                                       const DevBox& B, int b, int x, int y, int z, long long c,
+                                                       uint8_t tf)
+{
+    MomentAcc<float> acc;
+    if (B.vfluid && !((tf & FL_OVR) && K->s.fo)) {
+        const u16* __restrict__ sf = K->s.f;
+        const u16* __restrict__ sg = K->s.g;
+        const long long N = K->L.N;
+        const int sy = B.sy, sz = B.sz;
+#define MBG_MT16(q) \
+    acc.template add<q>(pullu<q, BF>(ct, sf, N, c, sy, sz, false), pullu<q, BF>(ct, sg, N, c, sy, sz, true));
+        MBG_UNROLL27(MBG_MT16)
+#undef MBG_MT16
+    } else {
+        acc = moments_cell<BF>(K, b, x, y, z, tf);
+    }
+    return acc;
+}
+
+template <bool BF>
+__global__ void __launch_bounds__(TILE_CELLS) k_qcorr16(const LowpK* __restrict__ K, const CodecTab ct,
+                                                        const Tile* __restrict__ tiles, float* __restrict__ qs)
+{
+    const LV16& L = K->L;
+    const Tile t = tiles[blockIdx.x];
+    const DevBox& B = L.box[t.box];
+    int x, y, z;
+    if (!tile_cell(B, t, x, y, z)) return;
+    const long long c = B.voff + val_lin(B, x, y, z);
+    const uint8_t tf = flag_at(L, B, x, y, z);
+    float qx = 0.f, qy = 0.f, qz = 0.f;
+    if (tf & FL_FLUID) {
+        const Macro<float> m =
+            moments_at<BF>(K, ct, B, t.box, x, y, z, c, tf).finish(K->ph.mesh_speed, K->ph.Rg, K->ph.cv);
+        qx = m.qcx;
+        qy = m.qcy;
+        qz = m.qcz;
+    }
+    qs[c] = qx;
+    qs[L.N + c] = qy;
+    qs[2 * L.N + c] = qz;
+}
+
+// face cells of the pad: the normal component of Q_corr there
+template <bool BF>
+__global__ void k_qhalo16(const LowpK* __restrict__ K, const HaloCell* __restrict__ hl, long long n,
+                          float* __restrict__ qs)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const HaloCell h = hl[e];
+    const LV16& L = K->L;
+    const DevBox& B = L.box[h.box];
+    const int out0 = h.x < 0 || h.x >= B.n[0], out1 = h.y < 0 || h.y >= B.n[1], out2 = h.z < 0 || h.z >= B.n[2];
+    if (out0 + out1 + out2 != 1) return;   // edges and corners are not on any gradient stencil
+    const int d = out0 ? 0 : out1 ? 1 : 2;
+    const long long hc = B.voff + val_lin(B, h.x, h.y, h.z);
+    int p[3] = {B.lo[0] + h.x, B.lo[1] + h.y, B.lo[2] + h.z};
+    float v = 0.f;
+    // outside the domain box the gradient is one-sided, so nothing reads it
+    if (p[0] >= L.dlo[0] && p[1] >= L.dlo[1] && p[2] >= L.dlo[2] && p[0] <= L.dhi[0] && p[1] <= L.dhi[1] &&
+        p[2] <= L.dhi[2] && (flag_at(L, B, h.x, h.y, h.z) & FL_FLUID)) {
+        const int o = owner_of(L, p);
+        if (o >= 0) {
+            const DevBox& O = L.box[o];
+            v = qs[d * L.N + O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2])];
+        } else {
+            const uint8_t tf = flag_at(L, B, h.x, h.y, h.z);
+            const Macro<float> m =
+                moments16_slow<BF>(K, h.box, h.x, h.y, h.z, tf).finish(K->ph.mesh_speed, K->ph.Rg, K->ph.cv);
+            v = d == 0 ? m.qcx : d == 1 ? m.qcy : m.qcz;
+        }
+    }
+    qs[d * L.N + hc] = v;
+}
+
+template <bool BF>
+__global__ void __launch_bounds__(TILE_CELLS, 4)
+    k_collide16(const LowpK* __restrict__ K, const CodecTab ct, const Lattice<float> lat,
+                const Tile* __restrict__ tiles, const float* __restrict__ qs)
+{
+    const LV16& L = K->L;
+    const Tile t = tiles[blockIdx.x];
+    const DevBox& B = L.box[t.box];
+    int x, y, z;
+    if (!tile_cell(B, t, x, y, z)) return;
+    const long long N = L.N;
+    const long long c = B.voff + val_lin(B, x, y, z);
+    const uint8_t tf = flag_at(L, B, x, y, z);
+    const u16* __restrict__ sfo = K->s.fo;
+    const u16* __restrict__ sgo = K->s.go;
+    u16* __restrict__ fB = K->fB;
+    u16* __restrict__ gB = K->gB;
+    const bool ovr = (tf & FL_OVR) && sfo;
+    if (!(tf & FL_FLUID)) {
+#define MBG_SOLC16(q)                                               \
+    {                                                               \
+        fB[q * N + c] = ovr ? sfo[q * N + c] : SENT16;              \
+        gB[q * N + c] = ovr ? sgo[q * N + c] : SENT16;              \
+    }
+        MBG_UNROLL27(MBG_SOLC16)
+#undef MBG_SOLC16
+        return;
+    }
+    const Phys32* __restrict__ PH = K->phys ? K->phys + B.phys : &K->ph;
+    const float Rg = K->ph.Rg, cv = K->ph.cv;
+    const Macro<float> m = moments_at<BF>(K, ct, B, t.box, x, y, z, c, tf).finish(K->ph.mesh_speed, Rg, cv);
+    const int sy = B.sy, sz = B.sz;
+    const float dqx = grad1(present(L, B, x, y, z, 0, 1), present(L, B, x, y, z, 0, -1), qs[c + 1], m.qcx,
+                            qs[c - 1], PH->idx[0]);
+    const float dqy = grad1(present(L, B, x, y, z, 1, 1), present(L, B, x, y, z, 1, -1), qs[N + c + sy], m.qcy,
+                            qs[N + c - sy], PH->idx[1]);
+    const float dqz = grad1(present(L, B, x, y, z, 2, 1), present(L, B, x, y, z, 2, -1), qs[2 * N + c + sz],
+                            m.qcz, qs[2 * N + c - sz], PH->idx[2]);
+    Equilibrium<float> E;
+    const float omega = build_equilibrium<float>(m, dqx, dqy, dqz, PH->nu, PH->alpha, PH->dt, Rg, cv, lat, E);
+    if (B.vfluid && !ovr) {
+        const u16* __restrict__ sf = K->s.f;
+        const u16* __restrict__ sg = K->s.g;
+#define MBG_RC16(q)                                                                                  \
+    {                                                                                                \
+        const float fq = pullu<q, BF>(ct, sf, N, c, sy, sz, false);                                  \
+        fB[q * N + c] = enc<BF>(ct, fmaf(omega, E.template feq<q>() - fq, fq), q, false);            \
+        const float gq = pullu<q, BF>(ct, sg, N, c, sy, sz, true);                                   \
+        gB[q * N + c] = enc<BF>(ct, fmaf(omega, E.template geq<q>(lat) - gq, gq), q, true);          \
+    }
+        MBG_UNROLL27(MBG_RC16)
+#undef MBG_RC16
+    } else {
+#define MBG_RG16(q)                                                                                  \
+    {                                                                                                \
+        const float fq = pull_gen<q, BF>(K, t.box, x, y, z, 0);                                      \
+        fB[q * N + c] = enc<BF>(ct, fmaf(omega, E.template feq<q>() - fq, fq), q, false);            \
+        const float gq = pull_gen<q, BF>(K, t.box, x, y, z, 1);                                      \
+        gB[q * N + c] = enc<BF>(ct, fmaf(omega, E.template geq<q>(lat) - gq, gq), q, true);          \
+    }
+        MBG_UNROLL27(MBG_RG16)
+#undef MBG_RG16
+    }
+}
+
 // streamed values of the uncovered ghost cells of a fine level
 template <bool BF>
 __global__ void k_ghost_stream16(const LowpK* __restrict__ K, const GhostCell* gl, long long n)
@@ -487,30 +652,33 @@ __global__ void k_ghost_stream16(const LowpK* __restrict__ K, const GhostCell* g
 #undef MBG_GS16
 }
 
-// explosion (conservative linear interpolation, as in mbg_fp64.cu) in FP32
+// explosion (conservative linear interpolation, as in mbg_fp64_amr.cu) in
+// FP32: one warp per fine ghost cell, lane q interpolating direction q, the
+// limiter factor of each axis the minimum over the 27 components (blocks of
+// four warps)
 template <bool BF>
-__device__ __forceinline__ float crse16(const LowpK* __restrict__ KC, const int p0[3], int d, int s_, int q,
-                                        bool g)
+__device__ __forceinline__ long long crse16_index(const LV16& C, const int p0[3], int d, int s_)
 {
     int p[3] = {p0[0], p0[1], p0[2]};
     p[d] += s_;
-    const LV16& C = KC->L;
     wrap_pos(C, p);
     const int o = owner_of(C, p);
-    if (o < 0) return 0.0f;
+    if (o < 0) return -1;
     const DevBox& O = C.box[o];
-    const u16* v = g ? KC->s.g : KC->s.f;
-    return dec<BF>(KC->ct, v[q * C.N + O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2])], q, g);
+    return O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2]);
 }
 
 template <bool BF>
 __global__ void k_explode16(const LowpK* __restrict__ KF, const LowpK* __restrict__ KC, const GhostCell* gl,
                             long long n, u16* fg, u16* gg)
 {
-    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n) return;
+    const long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int q = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const bool act = e < n && q < NQ;
+    __shared__ float sa[4][3][32];   // per warp: limiter candidates of each axis and direction
     const LV16& F = KF->L;
-    const GhostCell g = gl[e];
+    const LV16& C = KC->L;
+    const GhostCell g = gl[e < n ? e : 0];
     const DevBox& B = F.box[g.box];
     int fp[3] = {B.lo[0] + g.x, B.lo[1] + g.y, B.lo[2] + g.z};
     wrap_pos(F, fp);
@@ -518,39 +686,65 @@ __global__ void k_explode16(const LowpK* __restrict__ KF, const LowpK* __restric
     const float off[3] = {((fp[0] - 2 * cp[0]) + 0.5f) / 2.0f - 0.5f, ((fp[1] - 2 * cp[1]) + 0.5f) / 2.0f - 0.5f,
                           ((fp[2] - 2 * cp[2]) + 0.5f) / 2.0f - 0.5f};
     const long long gi = B.goff + fab_lin(B, g.x, g.y, g.z);
+    long long ix[7];
+    ix[0] = crse16_index<BF>(C, cp, 0, 0);
+    for (int d = 0; d < 3; ++d) {
+        ix[1 + 2 * d] = crse16_index<BF>(C, cp, d, -1);
+        ix[2 + 2 * d] = crse16_index<BF>(C, cp, d, 1);
+    }
     for (int lat = 0; lat < 2; ++lat) {
         const bool isg = lat == 1;
-        u16* out = isg ? gg : fg;
-        float alpha[3] = {1.f, 1.f, 1.f};
-        for (int d = 0; d < 3; ++d)
-            for (int q = 0; q < NQ; ++q) {
-                const float u0 = crse16<BF>(KC, cp, d, 0, q, isg);
-                const float up = crse16<BF>(KC, cp, d, 1, q, isg);
-                const float um = crse16<BF>(KC, cp, d, -1, q, isg);
-                const float cen = 0.5f * (up - um);
-                const float forw = 2.0f * (up - u0);
-                const float back = 2.0f * (u0 - um);
-                const float slp = (forw * back >= 0.f) ? fminf(fabsf(forw), fabsf(back)) : 0.f;
-                if (cen != 0.f) alpha[d] = fminf(alpha[d], fminf(slp, fabsf(cen)) / fabsf(cen));
-            }
-        for (int q = 0; q < NQ; ++q) {
-            const float u0 = crse16<BF>(KC, cp, 0, 0, q, isg);
-            const float cx = 0.5f * (crse16<BF>(KC, cp, 0, 1, q, isg) - crse16<BF>(KC, cp, 0, -1, q, isg));
-            const float cy = 0.5f * (crse16<BF>(KC, cp, 1, 1, q, isg) - crse16<BF>(KC, cp, 1, -1, q, isg));
-            const float cz = 0.5f * (crse16<BF>(KC, cp, 2, 1, q, isg) - crse16<BF>(KC, cp, 2, -1, q, isg));
-            out[q * F.NG + gi] = enc<BF>(
-                KF->ct, u0 + off[0] * (alpha[0] * cx) + off[1] * (alpha[1] * cy) + off[2] * (alpha[2] * cz), q, isg);
+        const u16* v = isg ? KC->s.g : KC->s.f;
+        float u[7];
+        for (int k = 0; k < 7; ++k) u[k] = (act && ix[k] >= 0) ? dec<BF>(KC->ct, v[q * C.N + ix[k]], q, isg) : 0.0f;
+        float alpha[3], c[3];
+        for (int d = 0; d < 3; ++d) {
+            const float um = u[1 + 2 * d], up = u[2 + 2 * d], u0 = u[0];
+            const float cen = 0.5f * (up - um);
+            const float forw = 2.0f * (up - u0);
+            const float back = 2.0f * (u0 - um);
+            const float slp = (forw * back >= 0.f) ? fminf(fabsf(forw), fabsf(back)) : 0.f;
+            float a = (act && cen != 0.f) ? fminf(slp, fabsf(cen)) / fabsf(cen) : 1.0f;
+            sa[w][d][q] = a;
+            c[d] = cen;
         }
+        __syncwarp();
+        for (int d = 0; d < 3; ++d) {
+            float a = 1.0f;
+            for (int l = 0; l < NQ; ++l) a = fminf(a, sa[w][d][l]);
+            alpha[d] = a;
+        }
+        __syncwarp();
+        if (act)
+            (isg ? gg : fg)[q * F.NG + gi] = enc<BF>(
+                KF->ct, u[0] + off[0] * (alpha[0] * c[0]) + off[1] * (alpha[1] * c[1]) + off[2] * (alpha[2] * c[2]),
+                q, isg);
     }
 }
 
+// streamed value of a runtime direction (the coalescence's fallback)
+template <bool BF>
+__device__ __noinline__ float pull16_rt(int q, const LowpK* __restrict__ K, int b, int x, int y, int z,
+                                        uint8_t tflag, int which)
+{
+    switch (q) {
+#define MBG_PRT16(qq) \
+    case qq: return pull16_slow<qq, BF>(K, b, x, y, z, tflag, which);
+        MBG_UNROLL27(MBG_PRT16)
+#undef MBG_PRT16
+    }
+    return -1.0f;
+}
+
 // coalescence: FP64 masked average of the 8 fine children into the override
-// buffer (advance) or the coarse state (initial average_down)
+// buffer (advance) or the coarse state (initial average_down); one thread per
+// (coarse cell, direction), blockIdx.y the direction
 template <bool BF>
 __global__ void k_coalesce16(const LowpK* __restrict__ KC, const LowpK* __restrict__ KF, const CoalesceCell* cl,
                              long long n, u16* fo, u16* go, int into_state)
 {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
     if (e >= n) return;
     const LV16& C = KC->L;
     const LV16& F = KF->L;
@@ -558,32 +752,27 @@ __global__ void k_coalesce16(const LowpK* __restrict__ KC, const LowpK* __restri
     const DevBox& O = C.box[cc.cbox];
     const DevBox& A = F.box[cc.fbox];
     const long long cell = O.voff + val_lin(O, cc.cx, cc.cy, cc.cz);
-    const uint8_t tf = flag_at(C, O, cc.cx, cc.cy, cc.cz);
-    const double small_num = 2.220446049250313e-16 * 1e10;
+    // the mask test |v - (-1)| > SMALL_NUM on the FP32 decoded value; the sum in FP64
+    const float small_num = (float)(2.220446049250313e-16 * 1e10);
     for (int lat = 0; lat < 2; ++lat) {
         const bool isg = lat == 1;
         const u16* v = isg ? KF->s.g : KF->s.f;
         const u16* vg = isg ? KF->s.gg : KF->s.fg;
-        u16* out = isg ? go : fo;
-        const u16* cA = isg ? KC->s.g : KC->s.f;
-#define MBG_CO16(q)                                                                                          \
-        {                                                                                                    \
-            double sum = 0.0, vol = 0.0;                                                                     \
-            for (int kr = 0; kr < 2; ++kr)                                                                   \
-                for (int jr = 0; jr < 2; ++jr)                                                               \
-                    for (int ir = 0; ir < 2; ++ir) {                                                         \
-                        const double fv =                                                                    \
-                            dec<BF>(KF->ct, fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg), q, isg); \
-                        if (fabs(fv - (-1.0)) > small_num) { sum += fv; vol += 1.0; }                        \
-                    }                                                                                        \
-            u16 r;                                                                                           \
-            if (vol > 0.0) r = enc<BF>(KC->ct, (float)(sum / vol), q, isg);                                  \
-            else if (into_state) r = cA[q * C.N + cell];                                                     \
-            else r = enc<BF>(KC->ct, pull16_slow<q, BF>(KC, cc.cbox, cc.cx, cc.cy, cc.cz, tf, isg ? 1 : 0), q, isg); \
-            out[q * C.N + cell] = r;                                                                         \
-        }
-        MBG_UNROLL27(MBG_CO16)
-#undef MBG_CO16
+        double sum = 0.0;
+        int vol = 0;
+        for (int kr = 0; kr < 2; ++kr)
+            for (int jr = 0; jr < 2; ++jr)
+                for (int ir = 0; ir < 2; ++ir) {
+                    const float fv =
+                        dec<BF>(KF->ct, fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg), q, isg);
+                    if (fabsf(fv + 1.0f) > small_num) { sum += (double)fv; ++vol; }
+                }
+        u16 r;
+        if (vol > 0) r = enc<BF>(KC->ct, (float)(sum / (double)vol), q, isg);
+        else if (into_state) r = (isg ? KC->s.g : KC->s.f)[q * C.N + cell];
+        else r = enc<BF>(KC->ct, pull16_rt<BF>(q, KC, cc.cbox, cc.cx, cc.cy, cc.cz, flag_at(C, O, cc.cx, cc.cy, cc.cz),
+                                               isg ? 1 : 0), q, isg);
+        (isg ? go : fo)[q * C.N + cell] = r;
     }
 }
 
@@ -668,6 +857,22 @@ void Lowp16<BF>::fused(const LowpK* k, const CodecTab& ct, const Lattice<float>&
     if (ntiles > 0) k_fused<BF><<<grid, FT_THREADS, 0, s>>>(k, ct, lat, t, ntiles);
 }
 template <bool BF>
+int Lowp16<BF>::fused_blocks_per_sm()
+{
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused<BF>, FT_THREADS, 0) != cudaSuccess) nb = 1;
+    return nb > 0 ? nb : 1;
+}
+template <bool BF>
+void Lowp16<BF>::two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
+                          int ntiles, const HaloCell* h, long long nh, float* qs, cudaStream_t s)
+{
+    if (ntiles == 0) return;
+    k_qcorr16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, tiles, qs);
+    if (nh > 0) k_qhalo16<BF><<<(unsigned)((nh + 127) / 128), 128, 0, s>>>(k, h, nh, qs);
+    k_collide16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs);
+}
+template <bool BF>
 void Lowp16<BF>::ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s)
 {
     if (n > 0) k_ghost_stream16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, gl, n);
@@ -676,13 +881,14 @@ template <bool BF>
 void Lowp16<BF>::explode(const LowpK* kf, const LowpK* kc, const GhostCell* gl, long long n, u16* fg, u16* gg,
                          cudaStream_t s)
 {
-    if (n > 0) k_explode16<BF><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(kf, kc, gl, n, fg, gg);
+    if (n > 0) k_explode16<BF><<<(unsigned)((n * 32 + 127) / 128), 128, 0, s>>>(kf, kc, gl, n, fg, gg);
 }
 template <bool BF>
 void Lowp16<BF>::coalesce(const LowpK* kc, const LowpK* kf, const CoalesceCell* cl, long long n, u16* fo, u16* go,
                           int into_state, cudaStream_t s)
 {
-    if (n > 0) k_coalesce16<BF><<<(unsigned)((n + 63) / 64), 64, 0, s>>>(kc, kf, cl, n, fo, go, into_state);
+    const dim3 grid((unsigned)((n + 127) / 128), NQ);
+    if (n > 0) k_coalesce16<BF><<<grid, 128, 0, s>>>(kc, kf, cl, n, fo, go, into_state);
 }
 template <bool BF>
 void Lowp16<BF>::encode(const LowpK* k, const Tile* tiles, int ntiles, const double* src, long long NV, u16* dst,

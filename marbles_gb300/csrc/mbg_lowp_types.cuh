@@ -50,6 +50,15 @@ struct FusedTile {
     short pad;
 };
 
+// host helpers of the layout (mbg_lowp.cu), shared with the batched domains
+// (mbg_batch.cu)
+constexpr int FUSED_ZC[3] = {4, 8, 16};   // plane runs of the fused step variants 1..3
+CodecTab make_codec(const mbg_params& p);
+Phys32 phys32(const mbg_params& p, double dt, const double idx[3]);
+long long pad_boxes(std::vector<DevBox>& box);
+std::vector<HaloCell> halo_cells(const std::vector<DevBox>& box);
+std::vector<FusedTile> fused_tiles(const std::vector<DevBox>& box, int zc);
+
 // kernel launchers, instantiated for FP16 (BF = false) and BF16 (BF = true)
 template <bool BF>
 struct Lowp16 {
@@ -57,6 +66,10 @@ struct Lowp16 {
     static void halo_periodic(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s);
     static void fused(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const FusedTile* t, int ntiles,
                       int grid, cudaStream_t s);
+    static int fused_blocks_per_sm();   // resident CTAs of the fused step per SM
+    // the two-pass step: Q_corr pass, pad of Q_corr, collision pass (3 launches)
+    static void two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
+                         int ntiles, const HaloCell* h, long long nh, float* qs, cudaStream_t s);
     static void ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s);
     static void explode(const LowpK* kf, const LowpK* kc, const GhostCell* gl, long long n, u16* fg, u16* gg,
                         cudaStream_t s);

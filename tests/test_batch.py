@@ -1,0 +1,89 @@
+"""Batched independent periodic domains (mbg_batch_*), 16-bit forms (GPU).
+
+Each domain is a Taylor-Green instance with its own cell counts, velocity
+and viscosity.  The batch must equal, bit for bit, the same domains run one
+per context in the same 16-bit form (same kernels, same rounding), and stay
+within the form's tolerance of the FP64 path, which is bit-identical to the
+oracle (test_parity_fp64.py)."""
+import math
+
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+# u relative to each domain's largest velocity: the slowest domains (v0 down
+# to 0.01) keep fewer significant bits of u in the stored deviation
+TOL = {1: {"rho": 1e-4, "u": 3e-3, "T": 1e-4}, 2: {"rho": 1e-3, "u": 3e-2, "T": 1e-3}}
+
+
+def _setup(prec, count=6, seed0=7):
+    import marbles_gb300 as M
+    doms = cases.batch_domains(count, seed0, sizes=(8, 12, 16, 24), nu_range=(0.15, 0.2))
+    states, singles, ref = [], [], []
+    for n, nu, v0 in doms:
+        p, levels = cases.tg_domain(*n, nu=nu, v0=v0)
+        o = cases.run_oracle(p, levels, 0)
+        f, g = o.get_state(0)
+        states.append((f, g))
+        c = M.Context(cases.mbg_params_from(p, prec))
+        c.define_level(0, levels[0], o.get_grown_flags(0))
+        c.set_state(0, f, g)
+        singles.append(c)
+        r = M.Context(cases.mbg_params_from(p, 0))
+        r.define_level(0, levels[0], o.get_grown_flags(0))
+        r.set_state(0, f, g)
+        ref.append(r)
+    common = cases.mbg_params_from(p, prec)
+    b = M.Batch(common, [(n, [0.0] * 3, [2 * math.pi] * 3, nu, nu) for n, nu, _ in doms])
+    b.set_state(np.concatenate([f for f, _ in states]), np.concatenate([g for _, g in states]))
+    return b, singles, ref, doms
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_batch_equals_single_domain_contexts(prec):
+    b, singles, _, _ = _setup(prec)
+    for steps in (1, 2, 3):          # an eager step, a graph replay, both
+        b.step(steps)
+        for c in singles:
+            c.step(steps)
+        fb, gb = b.get_state()
+        fs = np.concatenate([c.get_state(0)[0] for c in singles])
+        gs = np.concatenate([c.get_state(0)[1] for c in singles])
+        assert np.array_equal(fb, fs) and np.array_equal(gb, gs), steps
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_batch_against_fp64(prec):
+    b, _, ref, doms = _setup(prec)
+    b.step(20)
+    for r in ref:
+        r.step(20)
+    a = b.get_macro()
+    off = 0
+    worst = {"rho": 0.0, "u": 0.0, "T": 0.0}
+    for (n, _, _), r in zip(doms, ref):
+        vol = int(np.prod(n))
+        A = a[off * 19:(off + vol) * 19].reshape(19, vol)
+        R = r.get_macro(0).reshape(19, vol)
+        off += vol
+        worst["rho"] = max(worst["rho"], float(np.max(np.abs(A[0] - R[0]) / R[0])))
+        worst["T"] = max(worst["T"], float(np.max(np.abs(A[18] - R[18]) / R[18])))
+        worst["u"] = max(worst["u"], float(np.max(np.abs(A[1:4] - R[1:4])) / np.max(np.abs(R[1:4]))))
+    print("batch form", prec, "errors", worst)
+    assert all(worst[k] <= TOL[prec][k] for k in worst), worst
+
+
+def test_batch_autotune_keeps_state():
+    b, singles, _, _ = _setup(1, count=4, seed0=11)
+    b.step(2)
+    f0, g0 = b.get_state()
+    b.autotune(2)
+    f1, g1 = b.get_state()
+    assert np.array_equal(f0, f1) and np.array_equal(g0, g1)
+    v, ms = b.tuning()
+    assert 0 <= v < 4 and all(t > 0 for t in ms)
+    b.step(4)
+    assert np.isfinite(b.get_state()[0]).all()

@@ -117,3 +117,24 @@ def test_state_round_trip_and_sentinel(prec):
     eps = 2.0 ** -11 if prec == 1 else 2.0 ** -8
     live = ~sent
     assert np.max(np.abs(f2[live] - f[live]) / np.abs(f[live])) < 4 * eps
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_autotune_keeps_state(prec):
+    """The tuner times every step variant on the live data: the state is
+    bit-identical afterwards, a variant is chosen per level, and the tuned
+    steps stay within the form's tolerance."""
+    p, levels = cases.gaussian_pulse(nc=32, fine_lo=8, fine_hi=23, mgs=16, width=3.0, t0=0.1)
+    c64, c16 = _pair(p, levels, prec)
+    c64.step(2)
+    c16.step(2)
+    before = [c16.get_state(lev) for lev in range(len(levels))]
+    c16.autotune(2)
+    for lev in range(len(levels)):
+        f, g = c16.get_state(lev)
+        assert np.array_equal(f, before[lev][0]) and np.array_equal(g, before[lev][1])
+        v, ms = c16.tuning(lev)
+        assert 0 <= v < 4 and all(t > 0 for t in ms)
+    c64.step(18)
+    c16.step(18)
+    _check(_errors(c64, c16, levels), prec, TOL_PULSE_U[prec])
