@@ -143,11 +143,13 @@ def run_form(form, steps, warmup, device_index):
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(device_index) as clk:
         ctx.synchronize()
+        torch.cuda.nvtx.range_push("timed")   # profiler captures select this range
         e0.record(stream)
         for _ in range(steps):
             ctx.step(1)
         e1.record(stream)
         e1.synchronize()
+        torch.cuda.nvtx.range_pop()
     ms = e0.elapsed_time(e1)
     launches = ctx.launch_count() - n0
     timing = ctx.timing()
@@ -184,6 +186,166 @@ def run_form(form, steps, warmup, device_index):
     res["state_finite"] = finite
     d.close()
     return res
+
+
+def batch_states(doms, threads=None):
+    """Initial states of the batched Taylor-Green domains from the library's
+    drop-in driver (the reference's IC), [domain][q][cell] concatenated."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    import inputs
+    import marbles_gb300 as M
+
+    def one(d):
+        n, nu, v0 = d
+        drv = M.LBM(inputs.tg_domain(*n, nu=nu, v0=v0), ["lbm.precision=fp64"])
+        drv.prepare()
+        st = drv.initial_state(0)
+        drv.close()
+        return st
+
+    with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
+        states = list(ex.map(one, doms))
+    return states
+
+
+def run_batch(form, steps, warmup, device_index, count=256):
+    """Config 3: `count` independent periodic Taylor-Green domains (cell
+    counts from {16, 24, ..., 96} per axis, v0 ~ U[0.01, 0.08],
+    nu ~ U[0.002, 0.02], seeded), advanced together by the batched 16-bit
+    form, against the same domains as one FP64 context each."""
+    import ctypes as C
+    import math
+    import numpy as np
+    import torch
+    import inputs
+    import marbles_gb300 as M
+
+    doms = inputs.batch_domains(count)
+    states = batch_states(doms)
+    nv = sum(int(np.prod(n)) for n, _, _ in doms)
+    f = torch.empty(nv * M.NQ, dtype=torch.float64, pin_memory=True)
+    g = torch.empty(nv * M.NQ, dtype=torch.float64, pin_memory=True)
+    off = 0
+    for fs, gs in states:
+        f[off:off + fs.size] = torch.from_numpy(fs)
+        g[off:off + gs.size] = torch.from_numpy(gs)
+        off += fs.size
+    common = M.default_params()
+    common.precision = PRECISION[form]
+    common.rho_ref, common.t_ref = 1.0, 1.0 / 3.0
+    out = {"workload": "batch of %d periodic Taylor-Green domains (cells per axis from {16, 24, ..., 96}, "
+                       "v0 ~ U[0.01, 0.08], nu ~ U[0.002, 0.02], seeds 0..%d), %.1f M cells"
+                       % (count, count - 1, nv / 1e6)}
+    dp = C.POINTER(C.c_double)
+    lib = M.lib()
+    if form != "fp64":
+        b = M.Batch(common, [(n, [0.0] * 3, [2 * math.pi] * 3, nu, nu) for n, nu, _ in doms])
+        b._check(lib.mbg_batch_set_state(b.h, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
+        stream = torch.cuda.ExternalStream(b.stream())
+        b.step(warmup)
+        b.autotune(3)
+        b.step(2)
+        b.synchronize()
+        n0 = b.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with Clocks(device_index) as clk:
+            torch.cuda.nvtx.range_push("timed")
+            e0.record(stream)
+            b.step(steps)
+            e1.record(stream)
+            e1.synchronize()
+            torch.cuda.nvtx.range_pop()
+        ms = e0.elapsed_time(e1)
+        out.update({"form": form, "ms_per_step": ms / steps, "mlups": nv * steps / (ms * 1e-3) / 1e6,
+                    "gpu_launches": b.launch_count() - n0, "tuning": b.tuning(), "clocks": clk.summary(),
+                    "cells": nv})
+        # end to end: upload of the initial state, the steps, download of the state
+        b.synchronize()
+        t0 = time.perf_counter()
+        b._check(lib.mbg_batch_set_state(b.h, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
+        b.step(steps)
+        b._check(lib.mbg_batch_get_state(b.h, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+        wall = time.perf_counter() - t0
+        out["e2e"] = {"value": nv * steps / wall / 1e6, "unit": "MLUPS",
+                      "h2d_bytes_per_step": 2 * f.numel() * 8 / steps, "d2h_bytes_per_step": 2 * f.numel() * 8 / steps,
+                      "wall_s": wall}
+        out["state_finite"] = bool(torch.isfinite(f).all())
+        b.close()
+        return out
+    # FP64: one context per domain, launched one after another each step
+    ctxs = []
+    off = 0
+    for (n, nu, v0), (fs, gs) in zip(doms, states):
+        q = M.default_params()
+        q.n_cell[:] = n
+        q.prob_lo[:] = [0.0] * 3
+        q.prob_hi[:] = [2 * math.pi] * 3
+        q.is_periodic[:] = [1, 1, 1]
+        q.nu, q.alpha = nu, nu
+        c = M.Context(q)
+        c.define_level(0, np.array([[0, 0, 0, n[0] - 1, n[1] - 1, n[2] - 1]]), None)
+        c.set_state(0, fs, gs)
+        ctxs.append(c)
+    for _ in range(warmup):
+        for c in ctxs:
+            c.step(1)
+    for c in ctxs:
+        c.synchronize()
+    t0 = time.perf_counter()
+    with Clocks(device_index) as clk:
+        for _ in range(steps):
+            for c in ctxs:
+                c.step(1)
+        for c in ctxs:
+            c.synchronize()
+    wall = time.perf_counter() - t0
+    out.update({"form": "fp64, one context per domain", "ms_per_step": wall * 1e3 / steps,
+                "mlups": nv * steps / wall / 1e6, "clocks": clk.summary(), "cells": nv,
+                "timing": "host wall clock over all contexts' streams"})
+    for c in ctxs:
+        c.close()
+    return out
+
+
+def run_adjoint(steps, K, n=128, nu=0.01):
+    """Config 4: the FP64 adjoint on a 128^3 periodic box.  T0 = 1/3 + 0.005 G
+    (G a seeded unit-variance Gaussian field, correlation length 8 cells),
+    T_target from the next seed, nu = alpha = 0.01, `steps` steps,
+    checkpoints every K; loss 1/2 ||T_final - T_target||^2.  Device-timed
+    forward (with checkpoints) and backward (recomputation included)."""
+    import numpy as np
+    import torch
+    import inputs
+    import marbles_gb300 as M
+
+    p = M.default_params()
+    p.n_cell[:] = [n] * 3
+    p.prob_lo[:] = [0.0] * 3
+    p.prob_hi[:] = [float(n)] * 3
+    p.is_periodic[:] = [1, 1, 1]
+    p.nu, p.alpha = nu, nu
+    T0 = 1.0 / 3.0 + 0.005 * inputs.gaussian_field([n] * 3, 0, 8.0)
+    Tt = 1.0 / 3.0 + 0.005 * inputs.gaussian_field([n] * 3, 1, 8.0)
+    adj = M.Adjoint(p)
+    adj.forward(T0, 2, 1)              # warm-up
+    adj.backward(np.zeros(n ** 3))
+    stream = torch.cuda.ExternalStream(adj.stream())
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    e[0].record(stream)
+    Tf = adj.forward(T0, steps, K)
+    e[1].record(stream)
+    grad = adj.backward(Tf - Tt)
+    e[2].record(stream)
+    e[2].synchronize()
+    fwd, bwd = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    return {"workload": "adjoint of %d^3 periodic, %d steps, checkpoints every %d, nu = alpha = %g, "
+                        "T0 = 1/3 + 0.005 G (correlation length 8)" % (n, steps, K, nu),
+            "forward_ms": fwd, "backward_ms": bwd, "adjoint_over_forward": bwd / fwd,
+            "forward_mlups": n ** 3 * steps / (fwd * 1e-3) / 1e6,
+            "loss": 0.5 * float(np.sum((Tf - Tt) ** 2)), "gradient_finite": bool(np.isfinite(grad).all()),
+            "final_state_finite": bool(np.isfinite(Tf).all())}
 
 
 def roofline(res, form):
@@ -244,7 +406,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="all")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="pulse128", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="pulse128", choices=sorted(WORKLOADS) + ["batch256", "adjoint128"])
     a = ap.parse_args()
     _WL[0] = a.workload
     a.warmup = max(a.warmup, 3)
@@ -280,6 +442,32 @@ def main():
     import torch
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
+    if a.workload == "adjoint128":
+        if rank == 0:
+            r = run_adjoint(a.steps, 20)
+            print(json.dumps({"metric": "adjoint/forward cost", "value": r["adjoint_over_forward"], "unit": "ratio",
+                              "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+                              "ms_per_step": r["forward_ms"] / a.steps, "higher_is_better": False,
+                              "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                              "config": {"workload": r["workload"]}, "adjoint": r}))
+        return
+    if a.workload == "batch256":
+        forms = ["fp16", "fp64"] if a.form == "all" else a.form.split(",")
+        res = {}
+        for form in forms:
+            try:
+                res[form] = run_batch(form, a.steps, a.warmup, dev)
+            except Exception as ex:
+                res[form] = {"error": str(ex)[:300]}
+        if rank == 0:
+            h = res.get("fp16", {})
+            print(json.dumps({"metric": "MLUPS", "value": h.get("mlups"), "unit": "MLUPS", "n_gpus": world,
+                              "steps": a.steps, "warmup": a.warmup, "ms_per_step": h.get("ms_per_step"),
+                              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                              "data": "synthetic", "config": {"workload": h.get("workload"), "form": "fp16"},
+                              "e2e": h.get("e2e"), "gpu_launches": h.get("gpu_launches"),
+                              "clocks": h.get("clocks"), "forms": res}))
+        return
     forms = ["fp64", "fp16", "bf16"] if a.form == "all" else a.form.split(",")
     results = {}
     for form in forms:

@@ -221,6 +221,29 @@ void* mbg_batch_stream(const mbg_batch* b);
 const char* mbg_batch_last_error(const mbg_batch* b);
 void mbg_batch_destroy(mbg_batch* b);
 
+/* ---- adjoint of the FP64 step ----------------------------------------------
+ * No counterpart in the reference.  Gradient of a loss of the final
+ * temperature field with respect to the initial temperature field, on one
+ * fully periodic box (p->n_cell, prob_lo/hi, nu, alpha, dx_outer, dt_outer,
+ * adiabatic_exponent, m_bar; precision MBG_FP64).  The initial state is the
+ * equilibrium of (rho0, u0, T0(x)) as the reference's initializer builds it
+ * (IC.H:474-519); a step is the reference's stream + collide.
+ * mbg_adj_forward runs nsteps steps from T0 (host, one value per cell,
+ * x fastest), checkpointing every K steps, and returns the final temperature
+ * field (of the stored populations).  mbg_adj_backward takes dL/dT_final of
+ * the last forward run and returns dL/dT0: the hand-written discrete adjoint
+ * of every step, walked backwards segment by segment, each segment recomputed
+ * from its checkpoint; FP64 throughout.  Memory: about (2 + nsteps/K + K)
+ * states of 432 bytes per cell. */
+typedef struct mbg_adj mbg_adj;
+mbg_status mbg_adj_create(const mbg_params* p, double rho0, const double u0[3], void* cuda_stream, mbg_adj** out);
+mbg_status mbg_adj_forward(mbg_adj* a, const double* T0, int nsteps, int K, double* T_final);
+mbg_status mbg_adj_backward(mbg_adj* a, const double* dL_dTfinal, double* dL_dT0);
+long long mbg_adj_launch_count(const mbg_adj* a);
+void* mbg_adj_stream(const mbg_adj* a);
+const char* mbg_adj_last_error(const mbg_adj* a);
+void mbg_adj_destroy(mbg_adj* a);
+
 /* ---- step without device allocation --------------------------------------
  * No counterpart in the reference.  For callers that cannot let a library
  * allocate device memory: a host code that has given the GPU to its own

@@ -87,6 +87,17 @@ def lib():
         L.mbg_fillpatch.argtypes = [vp, C.c_int]
         L.mbg_average_down.argtypes = [vp, C.c_int, C.c_int]
         L.mbg_autotune.argtypes = [vp, C.c_int]
+        L.mbg_adj_create.argtypes = [C.POINTER(MbgParams), C.c_double, dp, vp, C.POINTER(vp)]
+        L.mbg_adj_forward.argtypes = [vp, dp, C.c_int, C.c_int, dp]
+        L.mbg_adj_backward.argtypes = [vp, dp, dp]
+        L.mbg_adj_launch_count.argtypes = [vp]
+        L.mbg_adj_launch_count.restype = C.c_longlong
+        L.mbg_adj_stream.argtypes = [vp]
+        L.mbg_adj_stream.restype = vp
+        L.mbg_adj_last_error.argtypes = [vp]
+        L.mbg_adj_last_error.restype = C.c_char_p
+        L.mbg_adj_destroy.argtypes = [vp]
+        L.mbg_adj_destroy.restype = None
         L.mbg_batch_create.argtypes = [C.POINTER(MbgParams), C.c_int, C.POINTER(MbgDomain), vp, C.POINTER(vp)]
         L.mbg_batch_cells.argtypes = [vp, C.POINTER(C.c_longlong)]
         L.mbg_batch_set_state.argtypes = [vp, dp, dp]
@@ -354,6 +365,75 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Adjoint:
+    """FP64 forward run and its discrete adjoint on one periodic box
+    (mbg_adj_*): T0 -> T_final, and dL/dT_final -> dL/dT0."""
+
+    def __init__(self, params, rho0=1.0, u0=(0.0, 0.0, 0.0), stream=None):
+        self.L = lib()
+        h = C.c_void_p()
+        u = np.ascontiguousarray(u0, dtype=np.float64)
+        st = self.L.mbg_adj_create(C.byref(params), float(rho0), _dp(u), stream, C.byref(h))
+        if st != 0:
+            raise MbgError("mbg_adj_create: %s: %s" % (STATUS.get(st, st), self.L.mbg_last_error(None).decode()))
+        self.h = h
+        self.n = int(params.n_cell[0]) * int(params.n_cell[1]) * int(params.n_cell[2])
+
+    def _check(self, st, what):
+        if st != 0:
+            raise MbgError("%s: %s: %s" % (what, STATUS.get(st, st), self.L.mbg_adj_last_error(self.h).decode()))
+
+    def forward(self, T0, nsteps, K):
+        T0 = np.ascontiguousarray(T0, dtype=np.float64).reshape(-1)
+        assert T0.size == self.n
+        out = np.empty(self.n)
+        self._check(self.L.mbg_adj_forward(self.h, _dp(T0), int(nsteps), int(K), _dp(out)), "mbg_adj_forward")
+        return out
+
+    def backward(self, dL_dTfinal):
+        g = np.ascontiguousarray(dL_dTfinal, dtype=np.float64).reshape(-1)
+        out = np.empty(self.n)
+        self._check(self.L.mbg_adj_backward(self.h, _dp(g), _dp(out)), "mbg_adj_backward")
+        return out
+
+    def launch_count(self):
+        return self.L.mbg_adj_launch_count(self.h)
+
+    def stream(self):
+        return self.L.mbg_adj_stream(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mbg_adj_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def temperature_evolution(adj, nsteps, K):
+    """A torch.autograd.Function over the C ABI: T0 (FP64 tensor, one value per
+    cell) -> T_final after nsteps steps; its backward is the library's
+    hand-written adjoint (mbg_adj_backward)."""
+    import torch
+
+    class _Evolve(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, T0):
+            out = adj.forward(T0.detach().cpu().numpy(), nsteps, K)
+            return torch.from_numpy(out).to(T0.device)
+
+        @staticmethod
+        def backward(ctx, grad):
+            g = adj.backward(grad.detach().cpu().numpy())
+            return torch.from_numpy(g).to(grad.device)
+
+    return _Evolve.apply
 
 
 class LBM:

@@ -26,6 +26,7 @@ UNITS = {
     "mbg_lowp_f16.cu": [],
     "mbg_lowp_bf16.cu": [],
     "mbg_batch.cu": [],
+    "mbg_adjoint.cu": [],
     "mbg_capi.cu": [],
     "lbm_driver.cu": [],
     "lbm_capi.cu": [],

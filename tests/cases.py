@@ -147,17 +147,4 @@ def tg_domain(nx, ny, nz, nu, v0):
     return p, [chop([0, 0, 0], [nx - 1, ny - 1, nz - 1], max(nx, ny, nz))]
 
 
-def batch_domains(count=256, seed0=0, sizes=tuple(range(16, 97, 8)), nu_range=(0.002, 0.02),
-                  v0_range=(0.01, 0.08)):
-    """Batched Taylor-Green instances: instance s draws, from
-    numpy.random.default_rng(seed0 + s), its three cell counts from `sizes`,
-    v0 and nu uniformly from the ranges.  Returns [(n_cell, nu, v0)]."""
-    import numpy as np
-    out = []
-    for s in range(count):
-        rng = np.random.default_rng(seed0 + s)
-        n = [int(v) for v in rng.choice(np.asarray(sizes), size=3)]
-        v0 = float(rng.uniform(*v0_range))
-        nu = float(rng.uniform(*nu_range))
-        out.append((n, nu, v0))
-    return out
+from inputs import batch_domains  # noqa: E402  (the batched Taylor-Green instances)

@@ -88,3 +88,44 @@ def sphere(nx=256, ny=128, nz=128, r=16.0, c=(64.0, 64.0, 64.0), maxlev=2, mgs=3
            mach=0.0670820):
     return SPHERE.format(nx=nx, ny=ny, nz=nz, r=r, cx=c[0], cy=c[1], cz=c[2], maxlev=maxlev, mgs=mgs, buf=buf,
                          nu=nu, mach=mach)
+
+
+def tg_domain(nx, ny, nz, nu, v0):
+    """One Taylor-Green domain on [0, 2 pi)^3, nx x ny x nz cells in one box."""
+    return (TG64.format(L=repr(2 * math.pi), n=nx, mgs=max(nx, ny, nz), w=repr(1.0 / math.pi))
+            .replace("amr.n_cell = %d %d %d" % (nx, nx, nx), "amr.n_cell = %d %d %d" % (nx, ny, nz))
+            .replace("lbm.nu = 0.005", "lbm.nu = %r" % nu)
+            .replace("ic_taylorgreen.v0 = 0.05", "ic_taylorgreen.v0 = %r" % v0))
+
+
+def batch_domains(count=256, seed0=0, sizes=tuple(range(16, 97, 8)), nu_range=(0.002, 0.02),
+                  v0_range=(0.01, 0.08)):
+    """Batched Taylor-Green instances: instance s draws, from
+    numpy.random.default_rng(seed0 + s), its three cell counts from `sizes`,
+    v0 and nu uniformly from the ranges.  Returns [(n_cell, nu, v0)]."""
+    import numpy as np
+    out = []
+    for s in range(count):
+        rng = np.random.default_rng(seed0 + s)
+        n = [int(v) for v in rng.choice(np.asarray(sizes), size=3)]
+        v0 = float(rng.uniform(*v0_range))
+        nu = float(rng.uniform(*nu_range))
+        out.append((n, nu, v0))
+    return out
+
+
+def gaussian_field(n, seed, corr=8.0):
+    """Seeded unit-variance Gaussian random field on a periodic grid n = (nx,
+    ny, nz), correlation length `corr` cells (white noise filtered by
+    exp(-k^2 corr^2 / 2) in Fourier space); returned x-fastest, flat."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal((n[2], n[1], n[0]))
+    kz = np.fft.fftfreq(n[2])[:, None, None] * 2 * np.pi
+    ky = np.fft.fftfreq(n[1])[None, :, None] * 2 * np.pi
+    kx = np.fft.rfftfreq(n[0])[None, None, :] * 2 * np.pi
+    filt = np.exp(-(kx ** 2 + ky ** 2 + kz ** 2) * corr ** 2 / 2)
+    gfield = np.fft.irfftn(np.fft.rfftn(w) * filt, s=w.shape)
+    gfield -= gfield.mean()
+    gfield /= gfield.std()
+    return gfield.reshape(-1)
