@@ -406,7 +406,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="all")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="pulse128", choices=sorted(WORKLOADS) + ["batch256", "adjoint128"])
+    ap.add_argument("--workload", default="pulse128", choices=sorted(WORKLOADS) + ["batch256", "batch32", "adjoint128"])
     a = ap.parse_args()
     _WL[0] = a.workload
     a.warmup = max(a.warmup, 3)
@@ -451,12 +451,12 @@ def main():
                               "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                               "config": {"workload": r["workload"]}, "adjoint": r}))
         return
-    if a.workload == "batch256":
+    if a.workload in ("batch256", "batch32"):
         forms = ["fp16", "fp64"] if a.form == "all" else a.form.split(",")
         res = {}
         for form in forms:
             try:
-                res[form] = run_batch(form, a.steps, a.warmup, dev)
+                res[form] = run_batch(form, a.steps, a.warmup, dev, count=int(a.workload[5:]))
             except Exception as ex:
                 res[form] = {"error": str(ex)[:300]}
         if rank == 0:
