@@ -13,7 +13,7 @@
 //
 // Reverse.  With s' = C(P(s)) (P the periodic pull, C the per-cell
 // collision, which couples neighbours only through dQ), one reverse step is
-//   k_adj_q  : Q_corr of the step's input state (recomputed),
+// (Q_corr of the step's input state kept from the segment's recomputation)
 //   k_adj_a1 : per cell, the transpose of the collision's Jacobian applied to
 //              the adjoint of the step's output: adjoints of the 14 moment
 //              sums reached through the macro fields, omega and the
@@ -116,24 +116,6 @@ __device__ __forceinline__ double dq_axis(const AdjBox& b, const double* Q, int 
     return (vp + vc + vm) * idx;
 }
 
-// runtime-direction g_eq of an Equilibrium (the same sums as geq<q>)
-__device__ __forceinline__ double geq_rt(const Equilibrium<double>& E, int q, const Lattice<double>& lat)
-{
-    const int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
-    double f = E.grho;
-    if (ex == 1) f = f + E.a1[0]; else if (ex == -1) f = f + (-E.a1[0]);
-    if (ey == 1) f = f + E.a1[1]; else if (ey == -1) f = f + (-E.a1[1]);
-    if (ez == 1) f = f + E.a1[2]; else if (ez == -1) f = f + (-E.a1[2]);
-    double s = E.A1[ex * ex] + E.A2[ey * ey];
-    if (ex * ey == 1) s = s + E.t3; else if (ex * ey == -1) s = s + (-E.t3);
-    s = s + E.A4[ez * ez];
-    if (ex * ez == 1) s = s + E.t5; else if (ex * ez == -1) s = s + (-E.t5);
-    if (ey * ez == 1) s = s + E.t6; else if (ey * ez == -1) s = s + (-E.t6);
-    f += 0.5 * s;
-    f *= lat.w[q];
-    return f;
-}
-
 // Reverse of the macro fields (MomentAcc::finish): adjoints of rho, U and T
 // (and a direct adjoint of 2 rho E) onto the moment sums rho, j, 2 rho E.
 __device__ __forceinline__ void macro_reverse(const MomentAcc<double>& acc, const Phys64& ph, double lrho,
@@ -157,12 +139,24 @@ __device__ __forceinline__ void macro_reverse(const MomentAcc<double>& acc, cons
 
 // Transpose of one cell's collision Jacobian (Source/LBM.cpp:621-807 and
 // Utilities.H:42-277 read backwards).  In: the moment sums of the pulled
-// values, dQ, the pulled values pf/pg and the adjoint of the outputs Lf/Lg.
+// values, dQ, the pulled values (re-read through P) and the adjoint of the
+// outputs Lf/Lg (component stride lstride).
 // Out: la[14] (adjoints of the moment sums, without the Q_corr part),
 // ldq[3], omega.
-__device__ void collide_reverse(const MomentAcc<double>& acc, const double dq[3], const Phys64& ph,
-                                const double* pf, const double* pg, const double* Lf, const double* Lg, double la[14],
-                                double ldq[3], double& omega_out)
+// the pulled values of one cell, read again from the state when needed
+struct CellPull {
+    const AdjBox* b;
+    int x, y, z;
+    const double *f, *g;
+    __device__ __forceinline__ long long src(int q) const
+    {
+        return q * b->N + nbr(*b, x, y, z, -ev_x(q), -ev_y(q), -ev_z(q));
+    }
+};
+
+__device__ void collide_reverse(const MomentAcc<double>& acc, const double dq[3], const Phys64& ph, const CellPull& P,
+                                const double* Lf, const double* Lg, long long lstride, double la[14], double ldq[3],
+                                double& omega_out)
 {
     const double ms = ph.mesh_speed, Rg = ph.Rg, cv = ph.cv, dt = ph.dt;
     const Lattice<double>& lat = ph.lat;
@@ -196,26 +190,34 @@ __device__ void collide_reverse(const MomentAcc<double>& acc, const double dq[3]
     double lw = 0.0;
     double lrf[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, lphz[3] = {0, 0, 0};
     double lgrho = 0.0, la1[3] = {0, 0, 0}, la2d[3] = {0, 0, 0}, la2o[3] = {0, 0, 0};
-    for (int q = 0; q < NQ; ++q) {
-        const int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
-        const double feq = E.rf[ex + 1][ey + 1] * E.phz[ez + 1];
-        const double geq = geq_rt(E, q, lat);
-        lw += Lf[q] * (feq - pf[q]) + Lg[q] * (geq - pg[q]);
-        const double lfe = omega * Lf[q];
-        lrf[ex + 1][ey + 1] += lfe * E.phz[ez + 1];
-        lphz[ez + 1] += lfe * E.rf[ex + 1][ey + 1];
-        const double wl = lat.w[q] * (omega * Lg[q]);
-        lgrho += wl;
-        la1[0] += ex * wl;
-        la1[1] += ey * wl;
-        la1[2] += ez * wl;
-        la2d[0] += 0.5 * lat.cth[ex * ex] * wl;
-        la2d[1] += 0.5 * lat.cth[ey * ey] * wl;
-        la2d[2] += 0.5 * lat.cth[ez * ez] * wl;
-        la2o[0] += ex * ey * wl;
-        la2o[1] += ex * ez * wl;
-        la2o[2] += ey * ez * wl;
+    // per direction, with compile-time lattice vectors (no int-to-double work)
+#define MBG_REV(q)                                                                                   \
+    {                                                                                                \
+        constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);                                      \
+        const double feq = E.rf[ex + 1][ey + 1] * E.phz[ez + 1];                                     \
+        const double geq = E.template geq<q>(lat);                                                   \
+        const long long si = P.src(q);                                                               \
+        const double lfq = Lf[q * lstride], lgq = Lg[q * lstride];                                   \
+        lw += lfq * (feq - P.f[si]) + lgq * (geq - P.g[si]);                                         \
+        const double lfe = omega * lfq;                                                              \
+        lrf[ex + 1][ey + 1] += lfe * E.phz[ez + 1];                                                  \
+        lphz[ez + 1] += lfe * E.rf[ex + 1][ey + 1];                                                  \
+        const double wl = lat.w[q] * (omega * lgq);                                                  \
+        lgrho += wl;                                                                                 \
+        if constexpr (ex == 1) la1[0] += wl; else if constexpr (ex == -1) la1[0] -= wl;              \
+        if constexpr (ey == 1) la1[1] += wl; else if constexpr (ey == -1) la1[1] -= wl;              \
+        if constexpr (ez == 1) la1[2] += wl; else if constexpr (ez == -1) la1[2] -= wl;              \
+        if constexpr (ex != 0) wd1[0] += wl; else wd0[0] += wl;                                      \
+        if constexpr (ey != 0) wd1[1] += wl; else wd0[1] += wl;                                      \
+        if constexpr (ez != 0) wd1[2] += wl; else wd0[2] += wl;                                      \
+        if constexpr (ex * ey == 1) la2o[0] += wl; else if constexpr (ex * ey == -1) la2o[0] -= wl;  \
+        if constexpr (ex * ez == 1) la2o[1] += wl; else if constexpr (ex * ez == -1) la2o[1] -= wl;  \
+        if constexpr (ey * ez == 1) la2o[2] += wl; else if constexpr (ey * ez == -1) la2o[2] -= wl;  \
     }
+    double wd0[3] = {0, 0, 0}, wd1[3] = {0, 0, 0};
+    MBG_UNROLL27(MBG_REV)
+#undef MBG_REV
+    for (int a = 0; a < 3; ++a) la2d[a] = 0.5 * (lat.cth[0] * wd0[a] + lat.cth[1] * wd1[a]);
     // ---- product-form f_eq ----
     double lrho = 0.0, lU[3] = {0, 0, 0}, lT = 0.0, ltre = 0.0, lwc = 0.0;
     double lph[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
@@ -434,12 +436,24 @@ __global__ void k_adj_temp(AdjBox b, Phys64 ph, const double* f, const double* g
     T[c] = acc.finish(ph.mesh_speed, ph.Rg, ph.cv).temp;
 }
 
-__device__ __forceinline__ void moments_to_pop(const double la[14], int q, double& lf, double& lg)
+// adjoint of one population from the adjoints of the moment sums (the
+// transpose of MomentAcc::add), compile-time lattice vector
+template <int q>
+__device__ __forceinline__ void moments_to_pop(const double la[14], double& lf, double& lg)
 {
-    const int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
-    lf = la[0] + ex * la[1] + ey * la[2] + ez * la[3] + (ex * ex) * la[4] + (ey * ey) * la[5] + (ez * ez) * la[6] +
-         (ex * ey) * la[7] + (ex * ez) * la[8] + (ey * ez) * la[9];
-    lg = la[10] + ex * la[11] + ey * la[12] + ez * la[13];
+    constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
+    double f = la[0], g = la[10];
+    if constexpr (ex == 1) { f += la[1]; g += la[11]; } else if constexpr (ex == -1) { f -= la[1]; g -= la[11]; }
+    if constexpr (ey == 1) { f += la[2]; g += la[12]; } else if constexpr (ey == -1) { f -= la[2]; g -= la[12]; }
+    if constexpr (ez == 1) { f += la[3]; g += la[13]; } else if constexpr (ez == -1) { f -= la[3]; g -= la[13]; }
+    if constexpr (ex != 0) f += la[4];
+    if constexpr (ey != 0) f += la[5];
+    if constexpr (ez != 0) f += la[6];
+    if constexpr (ex * ey == 1) f += la[7]; else if constexpr (ex * ey == -1) f -= la[7];
+    if constexpr (ex * ez == 1) f += la[8]; else if constexpr (ex * ez == -1) f -= la[8];
+    if constexpr (ey * ez == 1) f += la[9]; else if constexpr (ey * ez == -1) f -= la[9];
+    lf = f;
+    lg = g;
 }
 
 __global__ void k_adj_seed(AdjBox b, Phys64 ph, const double* f, const double* g, const double* dLdT, double* lf,
@@ -455,7 +469,9 @@ __global__ void k_adj_seed(AdjBox b, Phys64 ph, const double* f, const double* g
     double la[14] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const double lU[3] = {0, 0, 0};
     macro_reverse(acc, ph, 0.0, lU, dLdT[c], 0.0, la);
-    for (int q = 0; q < NQ; ++q) moments_to_pop(la, q, lf[q * b.N + c], lg[q * b.N + c]);
+#define MBG_SEEDQ(q) moments_to_pop<q>(la, lf[q * b.N + c], lg[q * b.N + c]);
+    MBG_UNROLL27(MBG_SEEDQ)
+#undef MBG_SEEDQ
 }
 
 // ---- reverse kernels -----------------------------------------------------
@@ -465,16 +481,11 @@ __global__ void __launch_bounds__(128) k_adj_a1(AdjBox b, Phys64 ph, const doubl
     int x, y, z;
     long long c;
     if (!adj_cell(b, x, y, z, c)) return;
-    double pf[NQ], pg[NQ], Lf[NQ], Lg[NQ];
-    const MomentAcc<double> acc = pulled_moments(b, x, y, z, f, g, pf, pg);
-    for (int q = 0; q < NQ; ++q) {
-        Lf[q] = lf[q * b.N + c];
-        Lg[q] = lg[q * b.N + c];
-    }
+    const MomentAcc<double> acc = pulled_moments(b, x, y, z, f, g, nullptr, nullptr);
     const double dq[3] = {dq_axis(b, Q, x, y, z, 0, ph.idx[0]), dq_axis(b, Q, x, y, z, 1, ph.idx[1]),
                           dq_axis(b, Q, x, y, z, 2, ph.idx[2])};
     double la[14], ldq[3], omega;
-    collide_reverse(acc, dq, ph, pf, pg, Lf, Lg, la, ldq, omega);
+    collide_reverse(acc, dq, ph, CellPull{&b, x, y, z, f, g}, lf + c, lg + c, b.N, la, ldq, omega);
     for (int i = 0; i < 14; ++i) ws[(WS_LA + i) * b.N + c] = la[i];
     for (int d = 0; d < 3; ++d) ws[(WS_LDQ + d) * b.N + c] = ldq[d];
     ws[WS_OMEGA * b.N + c] = omega;
@@ -539,14 +550,17 @@ __global__ void k_adj_a2(AdjBox b, Phys64 ph, const double* ws, const double* lf
     }
     macro_reverse(acc, ph, lrho, lU, lT, 0.0, la);
     const double om = 1.0 - ws[WS_OMEGA * b.N + c];
-    for (int q = 0; q < NQ; ++q) {
-        double mf, mg;
-        moments_to_pop(la, q, mf, mg);
-        // p(x, q) = s(x - e_q, q): push the adjoint back to its source
-        const long long t = nbr(b, x, y, z, -ev_x(q), -ev_y(q), -ev_z(q));
-        lfo[q * b.N + t] = om * lf[q * b.N + c] + mf;
-        lgo[q * b.N + t] = om * lg[q * b.N + c] + mg;
+    // p(x, q) = s(x - e_q, q): push each adjoint back to its source
+#define MBG_PUSH(q)                                                                \
+    {                                                                              \
+        double mf, mg;                                                             \
+        moments_to_pop<q>(la, mf, mg);                                             \
+        const long long t = nbr(b, x, y, z, -ev_x(q), -ev_y(q), -ev_z(q));         \
+        lfo[q * b.N + t] = om * lf[q * b.N + c] + mf;                              \
+        lgo[q * b.N + t] = om * lg[q * b.N + c] + mg;                              \
     }
+    MBG_UNROLL27(MBG_PUSH)
+#undef MBG_PUSH
 }
 
 }  // namespace mbg
@@ -568,6 +582,7 @@ struct mbg_adj {
     double *T0 = nullptr, *Tx = nullptr;
     std::vector<double*> ckpt;    // checkpoints, [f | g] each
     std::vector<double*> seg;     // states of the segment being reversed
+    std::vector<double*> segq;    // their Q_corr (computed by the recomputation)
     int cur = 0;
     int nsteps = -1, K = 0;
     long long launches = 0;
@@ -598,10 +613,11 @@ static mbg_status aalloc(mbg_adj* a, double** p, size_t count)
 
 static unsigned nblk(const mbg_adj* a) { return (unsigned)((a->b.N + 127) / 128); }
 
-static void fwd_step(mbg_adj* a, const double* f, const double* g, double* fo, double* go)
+static void fwd_step(mbg_adj* a, const double* f, const double* g, double* fo, double* go, double* Q = nullptr)
 {
-    k_adj_q<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, a->Q);
-    k_adj_step<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, a->Q, fo, go);
+    if (!Q) Q = a->Q;
+    k_adj_q<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, Q);
+    k_adj_step<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, Q, fo, go);
     a->launches += 2;
 }
 
@@ -714,10 +730,12 @@ mbg_status mbg_adj_backward(mbg_adj* a, const double* dL_dTfinal, double* dL_dT0
     const int K = a->K, nsteps = a->nsteps;
     // segment states
     while ((int)a->seg.size() < K) {
-        double* c = nullptr;
+        double *c = nullptr, *cq = nullptr;
         mbg_status st = aalloc(a, &c, 2 * N * NQ);
+        if (st == MBG_OK) st = aalloc(a, &cq, 3 * N);
         if (st != MBG_OK) return st;
         a->seg.push_back(c);
+        a->segq.push_back(cq);
     }
     // adjoint of the final state from dL/dT_final
     ACUDA(cudaMemcpyAsync(a->Tx, dL_dTfinal, N * sizeof(double), cudaMemcpyHostToDevice, a->s));
@@ -729,16 +747,21 @@ mbg_status mbg_adj_backward(mbg_adj* a, const double* dL_dTfinal, double* dL_dT0
         const int n0 = ci * K, n1 = std::min(nsteps, n0 + K);
         // recompute the segment's states from its checkpoint
         ACUDA(cudaMemcpyAsync(a->seg[0], a->ckpt[ci], 2 * N * NQ * sizeof(double), cudaMemcpyDeviceToDevice, a->s));
+        // (with the Q_corr of every state, which the reverse steps reuse)
         for (int i = 1; i < n1 - n0; ++i)
-            fwd_step(a, a->seg[i - 1], a->seg[i - 1] + N * NQ, a->seg[i], a->seg[i] + N * NQ);
+            fwd_step(a, a->seg[i - 1], a->seg[i - 1] + N * NQ, a->seg[i], a->seg[i] + N * NQ, a->segq[i - 1]);
+        {
+            const double* fl = a->seg[n1 - n0 - 1];
+            k_adj_q<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, fl, fl + N * NQ, a->segq[n1 - n0 - 1]);
+            a->launches++;
+        }
         for (int n = n1 - 1; n >= n0; --n) {
             const double* f = a->seg[n - n0];
             const double* g = f + N * NQ;
-            k_adj_q<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, a->Q);
-            k_adj_a1<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, a->Q, a->lf[lc], a->lg[lc], a->ws);
+            k_adj_a1<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, a->segq[n - n0], a->lf[lc], a->lg[lc], a->ws);
             k_adj_a2<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, a->ws, a->lf[lc], a->lg[lc], a->lf[1 - lc],
                                                  a->lg[1 - lc]);
-            a->launches += 3;
+            a->launches += 2;
             lc = 1 - lc;
         }
     }

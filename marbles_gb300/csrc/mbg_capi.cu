@@ -75,6 +75,10 @@ static const char* TK_NAMES[TK_N] = {"k_moments", "k_collide", "k_ghost_stream",
                                      "k_explode", "k_coalesce", "k_lowp_step", "k_halo", "other"};
 
 struct mbg_ctx {
+    // two coarse steps captured into a CUDA graph (see mbg_step)
+    cudaGraphExec_t graph = nullptr;
+    std::vector<int> graph_par;
+    long long graph_launches = 0;
     mbg_params p;
     bool timing = false;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> events;
@@ -93,6 +97,12 @@ struct mbg_ctx {
     size_t out19_n = 0;
     std::vector<void*> allocs;
 };
+
+static void drop_graph(mbg_ctx* ctx)
+{
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+}
 
 static std::string g_create_err;
 
@@ -319,6 +329,7 @@ mbg_status mbg_create(const mbg_params* params, void* cuda_stream, mbg_ctx** out
 
 void mbg_destroy(mbg_ctx* ctx)
 {
+    if (ctx) drop_graph(ctx);
     if (!ctx) return;
     if (ctx->s) cudaStreamSynchronize(ctx->s);
     drain_events(ctx);
@@ -347,6 +358,7 @@ long long mbg_launch_count(const mbg_ctx* ctx) { return ctx ? ctx->launches : 0;
 
 mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, const uint8_t* flags)
 {
+    if (ctx) drop_graph(ctx);
     if (!ctx) return MBG_EINVAL;
     if (lev != (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_define_level: levels must be defined in order 0, 1, ...");
     if (nbox <= 0 || !lohi) return fail(ctx, MBG_EINVAL, "mbg_define_level: need at least one box");
@@ -588,7 +600,18 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     Level& LL = ctx->lv.back();
     refresh_plan(ctx, LL);
     if (p.precision != MBG_FP64) {
-        mbg_status s2 = lowp_define(ctx->p, LL.plan, LL.hbox, LL.N, LL.NG, LL.dt, LL.idx, LL.lowp, ctx->err);
+        LevelHost host;
+        host.flags = &LL.hflags;
+        host.omap = &LL.omap;
+        host.ghosts = &ghosts;
+        for (int d = 0; d < 3; ++d) {
+            host.dlo[d] = LL.dlo[d];
+            host.dhi[d] = LL.dhi[d];
+            host.G[d] = LL.G[d];
+            host.nb[d] = LL.nb[d];
+            host.per[d] = ctx->p.is_periodic[d];
+        }
+        mbg_status s2 = lowp_define(ctx->p, LL.plan, LL.hbox, LL.N, LL.NG, LL.dt, LL.idx, host, LL.lowp, ctx->err);
         if (s2 != MBG_OK) return s2;
     }
     return MBG_OK;
@@ -750,11 +773,74 @@ static mbg_status time_step(mbg_ctx* ctx, int lev)
 
 extern "C" {
 
+// buffer parities of every level (both forms)
+static std::vector<int> parities(const mbg_ctx* ctx)
+{
+    std::vector<int> v;
+    for (const Level& L : ctx->lv) {
+        v.push_back(L.cur);
+        v.push_back(L.lowp.cur);
+    }
+    return v;
+}
+
+// Capture two coarse steps (every level advances an even number of times, so
+// the buffer parities come back to where they were) into a graph.  Nothing
+// runs during the capture; the host bookkeeping it performs is undone by
+// construction.  Returns false (and leaves no graph) if the capture fails.
+static bool capture_steps(mbg_ctx* ctx)
+{
+    drop_graph(ctx);
+    const std::vector<int> par0 = parities(ctx);
+    const long long l0 = ctx->launches;
+    if (cudaStreamBeginCapture(ctx->s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+    mbg_status st = MBG_OK;
+    for (int i = 0; i < 2 && st == MBG_OK; ++i) st = time_step(ctx, 0);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->s, &g);
+    const long long nl = ctx->launches - l0;
+    ctx->launches = l0;
+    if (st != MBG_OK || e != cudaSuccess || parities(ctx) != par0) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return false;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&ctx->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        ctx->graph = nullptr;
+        cudaGetLastError();
+        return false;
+    }
+    ctx->graph_par = par0;
+    ctx->graph_launches = nl;
+    return true;
+}
+
+// Without per-kernel timing, pairs of coarse steps replay a CUDA graph of
+// the whole subcycled hierarchy (captured on first use, re-captured when the
+// buffer parities differ from the capture's, e.g. after manual
+// advance/fillpatch calls); timing runs launch by launch.
 mbg_status mbg_step(mbg_ctx* ctx, int nsteps)
 {
     if (!ctx) return MBG_EINVAL;
     if (ctx->lv.empty()) return fail(ctx, MBG_ESTATE, "mbg_step: no level defined");
-    for (int i = 0; i < nsteps; ++i) {
+    int left = nsteps;
+    if (left >= 2 && !ctx->timing) {
+        // the first step runs eagerly (it uploads the constant blocks)
+        if (!ctx->graph || parities(ctx) != ctx->graph_par) {
+            mbg_status st = time_step(ctx, 0);
+            if (st != MBG_OK) return st;
+            --left;
+            if (left >= 2) capture_steps(ctx);
+        }
+        while (left >= 2 && ctx->graph && parities(ctx) == ctx->graph_par) {
+            MBG_CUDA(cudaGraphLaunch(ctx->graph, ctx->s));
+            ctx->launches += ctx->graph_launches;
+            left -= 2;
+        }
+    }
+    for (; left > 0; --left) {
         mbg_status st = time_step(ctx, 0);
         if (st != MBG_OK) return st;
     }
@@ -779,6 +865,7 @@ mbg_status mbg_fillpatch(mbg_ctx* ctx, int lev)
 mbg_status mbg_autotune(mbg_ctx* ctx, int reps)
 {
     if (!ctx) return MBG_EINVAL;
+    drop_graph(ctx);
     if (reps < 1) return fail(ctx, MBG_EINVAL, "mbg_autotune: reps must be >= 1");
     if (ctx->p.precision == MBG_FP64) return MBG_OK;
     const int nl = (int)ctx->lv.size();

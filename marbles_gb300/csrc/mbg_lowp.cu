@@ -31,6 +31,17 @@ struct LowpDev {
     double variant_ms[4] = {0, 0, 0, 0};   // tuner's timings (0: not timed)
     float* qs = nullptr;         // Q_corr of the two-pass step, [3][N]
     HaloCell* halo = nullptr;    // every pad cell of every box
+    long long* gdst = nullptr;   // pad fill by gather: destination and source indices
+    long long* gsrc = nullptr;
+    long long ngather = 0;
+    HaloCell* general = nullptr; // pad cells that need the general kernel (physical BCs)
+    long long ngeneral = 0;
+    long long* sdst = nullptr;   // ghost stream by gather (ghost_plan)
+    long long* ssrc = nullptr;
+    long long nsgather = 0;
+    int* scell = nullptr;        // ghost stream entries for the general kernel
+    int* sq = nullptr;
+    long long nsgen = 0;
     long long nhalo = 0;
     u16* fo = nullptr;           // coalescence override buffers
     u16* go = nullptr;
@@ -181,8 +192,130 @@ std::vector<FusedTile> fused_tiles(const std::vector<DevBox>& box, int zc)
     return tiles;
 }
 
+// Pad fill plan: for every (pad cell, inward direction) whose target is a
+// fluid cell and whose source is a fluid cell inside the domain, the storage
+// index the value is copied from -- a valid cell of the owning box (periodic
+// images resolved) as q N + index, or the box's own ghost fab as
+// -(q NG + index) - 1.  Pad cells with a source outside a non-periodic side
+// (physical BC) go to a separate list filled by the general kernel.
+static void halo_plan(const std::vector<DevBox>& box, const std::vector<HaloCell>& halo, long long N, long long NG,
+                      const LevelHost& h, std::vector<long long>& dst, std::vector<long long>& src,
+                      std::vector<HaloCell>& general)
+{
+    auto fab = [](const DevBox& B, int x, int y, int z) {
+        return ((long long)(z + 3) * (B.n[1] + 6) + (y + 3)) * (B.n[0] + 6) + (x + 3);
+    };
+    const std::vector<uint8_t>& fl = *h.flags;
+    for (const HaloCell& c : halo) {
+        const DevBox& B = box[c.box];
+        const uint8_t sf = fl[B.foff + fab(B, c.x, c.y, c.z)];
+        bool gen = false;
+        for (int q = 0; q < NQ && !gen; ++q) {
+            const int tx = c.x + ev_x(q), ty = c.y + ev_y(q), tz = c.z + ev_z(q);
+            if (tx < 0 || ty < 0 || tz < 0 || tx >= B.n[0] || ty >= B.n[1] || tz >= B.n[2]) continue;
+            if (!(fl[B.foff + fab(B, tx, ty, tz)] & FL_FLUID)) continue;   // target not collided
+            if (!(sf & FL_FLUID)) continue;                                   // bounce-back in the step
+            int gp[3] = {B.lo[0] + c.x, B.lo[1] + c.y, B.lo[2] + c.z};
+            bool out = false;
+            for (int d = 0; d < 3; ++d) {
+                if (gp[d] < h.dlo[d] || gp[d] > h.dhi[d]) {
+                    if (!h.per[d]) { out = true; break; }
+                    const int len = h.dhi[d] - h.dlo[d] + 1;
+                    gp[d] = h.dlo[d] + (((gp[d] - h.dlo[d]) % len) + len) % len;
+                }
+            }
+            if (out) { gen = true; break; }
+            const int bi = (gp[0] - h.dlo[0]) / h.G[0], bj = (gp[1] - h.dlo[1]) / h.G[1], bk = (gp[2] - h.dlo[2]) / h.G[2];
+            const int o = (*h.omap)[((size_t)bk * h.nb[1] + bj) * h.nb[0] + bi];
+            long long sidx;
+            if (o >= 0) {
+                const DevBox& O = box[o];
+                sidx = (long long)q * N + O.voff + (long long)(gp[2] - O.lo[2]) * O.sz +
+                       (long long)(gp[1] - O.lo[1]) * O.sy + (gp[0] - O.lo[0]);
+            } else if (B.goff >= 0) {
+                sidx = -((long long)q * NG + B.goff + fab(B, c.x, c.y, c.z)) - 1;
+            } else {
+                gen = true;
+                break;
+            }
+            dst.push_back((long long)q * N + B.voff + (long long)c.z * B.sz + (long long)c.y * B.sy + c.x);
+            src.push_back(sidx);
+        }
+        if (gen) general.push_back(c);
+    }
+}
+
+// Ghost-stream plan: for every uncovered ghost cell and direction, the
+// streamed value as a copy -- from a valid cell of the owning box (src >= 0,
+// q N + index), from the box's own ghost fab (src = -(q NG + index) - 2) --
+// or the -1 sentinel (src = -1).  Bounce-back from a solid source (a value
+// of the opposite direction, re-encoded) and physical BCs go to the general
+// list as (ghost-cell index, direction).
+static void ghost_plan(const std::vector<DevBox>& box, const std::vector<GhostCell>& gl, long long N, long long NG,
+                       const LevelHost& h, std::vector<long long>& dst, std::vector<long long>& src,
+                       std::vector<int>& gen_cell, std::vector<int>& gen_q)
+{
+    auto fab = [](const DevBox& B, int x, int y, int z) {
+        return ((long long)(z + 3) * (B.n[1] + 6) + (y + 3)) * (B.n[0] + 6) + (x + 3);
+    };
+    const std::vector<uint8_t>& fl = *h.flags;
+    for (size_t e = 0; e < gl.size(); ++e) {
+        const GhostCell& c = gl[e];
+        const DevBox& B = box[c.box];
+        const long long gi = B.goff + fab(B, c.x, c.y, c.z);
+        const uint8_t tf = fl[B.foff + fab(B, c.x, c.y, c.z)];
+        for (int q = 0; q < NQ; ++q) {
+            const long long d = (long long)q * NG + gi;
+            const int sx = c.x - ev_x(q), sy = c.y - ev_y(q), sz = c.z - ev_z(q);
+            if (!(tf & FL_FLUID) || sx < -3 || sy < -3 || sz < -3 || sx > B.n[0] + 2 || sy > B.n[1] + 2 ||
+                sz > B.n[2] + 2) {
+                dst.push_back(d);
+                src.push_back(-1);
+                continue;
+            }
+            if (!(fl[B.foff + fab(B, sx, sy, sz)] & FL_FLUID)) {
+                gen_cell.push_back((int)e);
+                gen_q.push_back(q);
+                continue;
+            }
+            int gp[3] = {B.lo[0] + sx, B.lo[1] + sy, B.lo[2] + sz};
+            bool out = false;
+            for (int a = 0; a < 3; ++a) {
+                if (gp[a] < h.dlo[a] || gp[a] > h.dhi[a]) {
+                    if (!h.per[a]) { out = true; break; }
+                    const int len = h.dhi[a] - h.dlo[a] + 1;
+                    gp[a] = h.dlo[a] + (((gp[a] - h.dlo[a]) % len) + len) % len;
+                }
+            }
+            if (out) {
+                gen_cell.push_back((int)e);
+                gen_q.push_back(q);
+                continue;
+            }
+            long long sidx = -1;
+            if (sx >= 0 && sy >= 0 && sz >= 0 && sx < B.n[0] && sy < B.n[1] && sz < B.n[2]) {
+                sidx = (long long)q * N + B.voff + (long long)sz * B.sz + (long long)sy * B.sy + sx;
+            } else {
+                const int bi = (gp[0] - h.dlo[0]) / h.G[0], bj = (gp[1] - h.dlo[1]) / h.G[1],
+                          bk = (gp[2] - h.dlo[2]) / h.G[2];
+                const int o = (*h.omap)[((size_t)bk * h.nb[1] + bj) * h.nb[0] + bi];
+                if (o >= 0) {
+                    const DevBox& O = box[o];
+                    sidx = (long long)q * N + O.voff + (long long)(gp[2] - O.lo[2]) * O.sz +
+                           (long long)(gp[1] - O.lo[1]) * O.sy + (gp[0] - O.lo[0]);
+                } else if (B.goff >= 0) {
+                    sidx = -((long long)q * NG + B.goff + fab(B, sx, sy, sz)) - 2;
+                }
+            }
+            dst.push_back(d);
+            src.push_back(sidx);
+        }
+    }
+}
+
 mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::vector<DevBox>& hbox, long long N,
-                       long long NG, double dt, const double idx[3], LowpLevel& L, std::string& err)
+                       long long NG, double dt, const double idx[3], const LevelHost& host, LowpLevel& L,
+                       std::string& err)
 {
     L.precision = p.precision;
     L.NV = N;
@@ -196,6 +329,12 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     for (size_t n = 0; n < box.size(); ++n) box[n].hoff = hbox[n].voff;
     L.N = pad_boxes(box);
     const std::vector<HaloCell> halo = halo_cells(box);
+    std::vector<long long> gdst, gsrc;
+    std::vector<HaloCell> general;
+    halo_plan(box, halo, L.N, NG, host, gdst, gsrc, general);
+    std::vector<long long> sdst, ssrc;
+    std::vector<int> scell, sq;
+    if (host.ghosts && NG > 0) ghost_plan(box, *host.ghosts, L.N, NG, host, sdst, ssrc, scell, sq);
     D->nhalo = (long long)halo.size();
     mbg_status st;
     if ((st = lalloc(L, (void**)&D->box16, box.size() * sizeof(DevBox), err)) != MBG_OK) return st;
@@ -206,6 +345,24 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
         cudaMemcpy(D->ftiles[v], tiles.data(), tiles.size() * sizeof(FusedTile), cudaMemcpyHostToDevice);
     }
     if ((st = lalloc(L, (void**)&D->halo, halo.size() * sizeof(HaloCell), err)) != MBG_OK) return st;
+    D->ngather = (long long)gdst.size();
+    D->ngeneral = (long long)general.size();
+    if ((st = lalloc(L, (void**)&D->gdst, gdst.size() * sizeof(long long), err)) != MBG_OK) return st;
+    if ((st = lalloc(L, (void**)&D->gsrc, gsrc.size() * sizeof(long long), err)) != MBG_OK) return st;
+    if ((st = lalloc(L, (void**)&D->general, general.size() * sizeof(HaloCell), err)) != MBG_OK) return st;
+    cudaMemcpy(D->gdst, gdst.data(), gdst.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    cudaMemcpy(D->gsrc, gsrc.data(), gsrc.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    cudaMemcpy(D->general, general.data(), general.size() * sizeof(HaloCell), cudaMemcpyHostToDevice);
+    D->nsgather = (long long)sdst.size();
+    D->nsgen = (long long)scell.size();
+    if ((st = lalloc(L, (void**)&D->sdst, sdst.size() * sizeof(long long), err)) != MBG_OK) return st;
+    if ((st = lalloc(L, (void**)&D->ssrc, ssrc.size() * sizeof(long long), err)) != MBG_OK) return st;
+    if ((st = lalloc(L, (void**)&D->scell, scell.size() * sizeof(int), err)) != MBG_OK) return st;
+    if ((st = lalloc(L, (void**)&D->sq, sq.size() * sizeof(int), err)) != MBG_OK) return st;
+    cudaMemcpy(D->sdst, sdst.data(), sdst.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    cudaMemcpy(D->ssrc, ssrc.data(), ssrc.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    cudaMemcpy(D->scell, scell.data(), scell.size() * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(D->sq, sq.data(), sq.size() * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(D->box16, box.data(), box.size() * sizeof(DevBox), cudaMemcpyHostToDevice);
     cudaMemcpy(D->halo, halo.data(), halo.size() * sizeof(HaloCell), cudaMemcpyHostToDevice);
     const size_t sb = (size_t)L.N * NQ * 2;
@@ -364,11 +521,16 @@ int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const Le
         ++launches;
     }
     if (D->nhalo > 0) {
-        run(LOWP_STAGE_HALO, [&] { LOWP16(bf, halo, k, D->halo, D->nhalo, s); });
+        run(LOWP_STAGE_HALO, [&] {
+            LOWP16(bf, halo_gather, k, D->gdst, D->gsrc, D->ngather, s);
+            LOWP16(bf, halo, k, D->general, D->ngeneral, s);
+        });
         ++launches;
     }
     if (L.NG > 0 && plan.nghost_cells > 0) {
-        run(LOWP_STAGE_GHOST_STREAM, [&] { LOWP16(bf, ghost_stream, k, plan.ghost_list, plan.nghost_cells, s); });
+        run(LOWP_STAGE_GHOST_STREAM, [&] {
+            LOWP16(bf, ghost_gather, k, D->sdst, D->ssrc, D->nsgather, plan.ghost_list, D->scell, D->sq, D->nsgen, s);
+        });
         ++launches;
     }
     if (D->variant == 0) {

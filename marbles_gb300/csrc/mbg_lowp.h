@@ -26,8 +26,17 @@ struct LowpLevel {
     std::vector<void*> allocs;
 };
 
+// host copy of a level's geometry, for the plans built at definition time
+struct LevelHost {
+    const std::vector<uint8_t>* flags;   // one byte per cell of each box grown by 3
+    const std::vector<int>* omap;        // owner of each G^3 bin, or -1
+    const std::vector<GhostCell>* ghosts;   // uncovered ghost cells (fine levels)
+    int dlo[3], dhi[3], G[3], nb[3], per[3];
+};
+
 mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::vector<DevBox>& hbox, long long N,
-                       long long NG, double dt, const double idx[3], LowpLevel& L, std::string& err);
+                       long long NG, double dt, const double idx[3], const LevelHost& host, LowpLevel& L,
+                       std::string& err);
 void lowp_release(LowpLevel& L);
 mbg_status lowp_set_state(LowpLevel& L, const LevelPlan& plan, const std::vector<DevBox>& hbox, const double* f,
                           const double* g, cudaStream_t s, std::string& err);

@@ -174,6 +174,24 @@ __global__ void k_halo16(const LowpK* __restrict__ K, const HaloCell* __restrict
 #undef MBG_HF16
 }
 
+// pad fill by gather (the plan of mbg_lowp.cu::halo_plan): a copy of f and
+// g from a valid cell (src >= 0) or the box's ghost fab (src < 0)
+template <bool BF>
+__global__ void k_halo_gather16(const LowpK* __restrict__ K, const long long* __restrict__ dst,
+                                const long long* __restrict__ src, long long n)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const long long d = dst[e], s_ = src[e];
+    if (s_ >= 0) {
+        K->fA[d] = K->s.f[s_];
+        K->gA[d] = K->s.g[s_];
+    } else {
+        K->fA[d] = K->s.fg[-s_ - 1];
+        K->gA[d] = K->s.gg[-s_ - 1];
+    }
+}
+
 // pad of self-periodic boxes (batched independent domains): a copy of the
 // opposite face, edge or corner of the same box
 template <bool BF>
@@ -479,14 +497,25 @@ __global__ void __launch_bounds__(FT_THREADS, 2)
 // box-local cell of thread threadIdx.x of a Tile (128 cells in x-fastest order)
 __device__ __forceinline__ bool tile_cell(const DevBox& B, const Tile& t, int& x, int& y, int& z)
 {
-    const long long ci = (long long)t.start + threadIdx.x;
-    const long long nxy = (long long)B.n[0] * B.n[1];
-    if (ci >= nxy * B.n[2]) return false;
+    // boxes hold fewer than 2^31 cells: 32-bit division
+    const unsigned ci = (unsigned)t.start + threadIdx.x;
+    const unsigned nxy = (unsigned)B.n[0] * (unsigned)B.n[1];
+    if (ci >= nxy * (unsigned)B.n[2]) return false;
     z = (int)(ci / nxy);
-    const int r = (int)(ci - (long long)z * nxy);
-    y = r / B.n[0];
-    x = r - y * B.n[0];
+    const unsigned r = ci - (unsigned)z * nxy;
+    y = (int)(r / (unsigned)B.n[0]);
+    x = (int)(r - (unsigned)y * (unsigned)B.n[0]);
     return true;
+}
+
+// present() for a box whose cells one layer out are all fluid: only the
+// domain bounds (and the box itself for a domain of its own) matter
+__device__ __forceinline__ bool present_vf(const LV16& L, const DevBox& B, int c, int d, int s)
+{
+    const int p = c + s;
+    const int gd = B.lo[d] + p;
+    if (gd < L.dlo[d] || gd > L.dhi[d]) return false;
+    return !(B.own_domain && (p < 0 || p >= B.n[d]));
 }
 
 template <bool BF>
@@ -557,10 +586,16 @@ __global__ void k_qhalo16(const LowpK* __restrict__ K, const HaloCell* __restric
         if (o >= 0) {
             const DevBox& O = L.box[o];
             v = qs[d * L.N + O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2])];
-        } else {
-            const uint8_t tf = flag_at(L, B, h.x, h.y, h.z);
-            const Macro<float> m =
-                moments16_slow<BF>(K, h.box, h.x, h.y, h.z, tf).finish(K->ph.mesh_speed, K->ph.Rg, K->ph.cv);
+        } else if (B.goff >= 0) {
+            // coarse-fine ghost: moments of the values the ghost stream of
+            // this advance has just written into the destination's ghost fab
+            const long long gi = B.goff + fab_lin(B, h.x, h.y, h.z);
+            MomentAcc<float> acc;
+#define MBG_QG16(q) \
+    acc.template add<q>(dec<BF>(K->ct, K->fBg[q * L.NG + gi], q, false), dec<BF>(K->ct, K->gBg[q * L.NG + gi], q, true));
+            MBG_UNROLL27(MBG_QG16)
+#undef MBG_QG16
+            const Macro<float> m = acc.finish(K->ph.mesh_speed, K->ph.Rg, K->ph.cv);
             v = d == 0 ? m.qcx : d == 1 ? m.qcy : m.qcz;
         }
     }
@@ -568,7 +603,7 @@ __global__ void k_qhalo16(const LowpK* __restrict__ K, const HaloCell* __restric
 }
 
 template <bool BF>
-__global__ void __launch_bounds__(TILE_CELLS, 4)
+__global__ void __launch_bounds__(TILE_CELLS, 5)
     k_collide16(const LowpK* __restrict__ K, const CodecTab ct, const Lattice<float> lat,
                 const Tile* __restrict__ tiles, const float* __restrict__ qs)
 {
@@ -599,12 +634,19 @@ __global__ void __launch_bounds__(TILE_CELLS, 4)
     const float Rg = K->ph.Rg, cv = K->ph.cv;
     const Macro<float> m = moments_at<BF>(K, ct, B, t.box, x, y, z, c, tf).finish(K->ph.mesh_speed, Rg, cv);
     const int sy = B.sy, sz = B.sz;
-    const float dqx = grad1(present(L, B, x, y, z, 0, 1), present(L, B, x, y, z, 0, -1), qs[c + 1], m.qcx,
-                            qs[c - 1], PH->idx[0]);
-    const float dqy = grad1(present(L, B, x, y, z, 1, 1), present(L, B, x, y, z, 1, -1), qs[N + c + sy], m.qcy,
-                            qs[N + c - sy], PH->idx[1]);
-    const float dqz = grad1(present(L, B, x, y, z, 2, 1), present(L, B, x, y, z, 2, -1), qs[2 * N + c + sz],
-                            m.qcz, qs[2 * N + c - sz], PH->idx[2]);
+    bool pr[6];
+    if (B.vfluid) {
+        pr[0] = present_vf(L, B, x, 0, 1); pr[1] = present_vf(L, B, x, 0, -1);
+        pr[2] = present_vf(L, B, y, 1, 1); pr[3] = present_vf(L, B, y, 1, -1);
+        pr[4] = present_vf(L, B, z, 2, 1); pr[5] = present_vf(L, B, z, 2, -1);
+    } else {
+        pr[0] = present(L, B, x, y, z, 0, 1); pr[1] = present(L, B, x, y, z, 0, -1);
+        pr[2] = present(L, B, x, y, z, 1, 1); pr[3] = present(L, B, x, y, z, 1, -1);
+        pr[4] = present(L, B, x, y, z, 2, 1); pr[5] = present(L, B, x, y, z, 2, -1);
+    }
+    const float dqx = grad1(pr[0], pr[1], qs[c + 1], m.qcx, qs[c - 1], PH->idx[0]);
+    const float dqy = grad1(pr[2], pr[3], qs[N + c + sy], m.qcy, qs[N + c - sy], PH->idx[1]);
+    const float dqz = grad1(pr[4], pr[5], qs[2 * N + c + sz], m.qcz, qs[2 * N + c - sz], PH->idx[2]);
     Equilibrium<float> E;
     const float omega = build_equilibrium<float>(m, dqx, dqy, dqz, PH->nu, PH->alpha, PH->dt, Rg, cv, lat, E);
     if (B.vfluid && !ovr) {
@@ -650,6 +692,48 @@ __global__ void k_ghost_stream16(const LowpK* __restrict__ K, const GhostCell* g
     }
     MBG_UNROLL27(MBG_GS16)
 #undef MBG_GS16
+}
+
+// ghost stream by gather (mbg_lowp.cu::ghost_plan) into the destination's
+// ghost fab
+template <bool BF>
+__global__ void k_ghost_gather16(const LowpK* __restrict__ K, const long long* __restrict__ dst,
+                                 const long long* __restrict__ src, long long n)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const long long d = dst[e], s_ = src[e];
+    u16 vf = SENT16, vg = SENT16;
+    if (s_ >= 0) {
+        vf = K->s.f[s_];
+        vg = K->s.g[s_];
+    } else if (s_ <= -2) {
+        vf = K->s.fg[-s_ - 2];
+        vg = K->s.gg[-s_ - 2];
+    }
+    K->fBg[d] = vf;
+    K->gBg[d] = vg;
+}
+
+template <bool BF>
+__device__ __noinline__ float pull16_rt(int q, const LowpK* __restrict__ K, int b, int x, int y, int z,
+                                        uint8_t tflag, int which);
+
+// the ghost stream's remaining entries (bounce-back, physical BCs)
+template <bool BF>
+__global__ void k_ghost_general16(const LowpK* __restrict__ K, const GhostCell* __restrict__ gl,
+                                  const int* __restrict__ gcell, const int* __restrict__ gq, long long n)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const GhostCell gc = gl[gcell[e]];
+    const int q = gq[e];
+    const LV16& L = K->L;
+    const DevBox& B = L.box[gc.box];
+    const uint8_t tf = flag_at(L, B, gc.x, gc.y, gc.z);
+    const long long gi = B.goff + fab_lin(B, gc.x, gc.y, gc.z);
+    K->fBg[q * L.NG + gi] = enc<BF>(K->ct, pull16_rt<BF>(q, K, gc.box, gc.x, gc.y, gc.z, tf, 0), q, false);
+    K->gBg[q * L.NG + gi] = enc<BF>(K->ct, pull16_rt<BF>(q, K, gc.box, gc.x, gc.y, gc.z, tf, 1), q, true);
 }
 
 // explosion (conservative linear interpolation, as in mbg_fp64_amr.cu) in
@@ -846,6 +930,11 @@ void Lowp16<BF>::halo(const LowpK* k, const HaloCell* h, long long n, cudaStream
     if (n > 0) k_halo16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, h, n);
 }
 template <bool BF>
+void Lowp16<BF>::halo_gather(const LowpK* k, const long long* dst, const long long* src, long long n, cudaStream_t s)
+{
+    if (n > 0) k_halo_gather16<BF><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(k, dst, src, n);
+}
+template <bool BF>
 void Lowp16<BF>::halo_periodic(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s)
 {
     if (n > 0) k_halo_periodic16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, h, n);
@@ -876,6 +965,13 @@ template <bool BF>
 void Lowp16<BF>::ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s)
 {
     if (n > 0) k_ghost_stream16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, gl, n);
+}
+template <bool BF>
+void Lowp16<BF>::ghost_gather(const LowpK* k, const long long* dst, const long long* src, long long n,
+                              const GhostCell* gl, const int* gcell, const int* gq, long long ngen, cudaStream_t s)
+{
+    if (n > 0) k_ghost_gather16<BF><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(k, dst, src, n);
+    if (ngen > 0) k_ghost_general16<BF><<<(unsigned)((ngen + 127) / 128), 128, 0, s>>>(k, gl, gcell, gq, ngen);
 }
 template <bool BF>
 void Lowp16<BF>::explode(const LowpK* kf, const LowpK* kc, const GhostCell* gl, long long n, u16* fg, u16* gg,

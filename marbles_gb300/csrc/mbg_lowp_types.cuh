@@ -63,6 +63,7 @@ std::vector<FusedTile> fused_tiles(const std::vector<DevBox>& box, int zc);
 template <bool BF>
 struct Lowp16 {
     static void halo(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s);
+    static void halo_gather(const LowpK* k, const long long* dst, const long long* src, long long n, cudaStream_t s);
     static void halo_periodic(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s);
     static void fused(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const FusedTile* t, int ntiles,
                       int grid, cudaStream_t s);
@@ -71,6 +72,9 @@ struct Lowp16 {
     static void two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
                          int ntiles, const HaloCell* h, long long nh, float* qs, cudaStream_t s);
     static void ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s);
+    // the ghost stream through its plan: gather, then the general entries
+    static void ghost_gather(const LowpK* k, const long long* dst, const long long* src, long long n,
+                             const GhostCell* gl, const int* gcell, const int* gq, long long ngen, cudaStream_t s);
     static void explode(const LowpK* kf, const LowpK* kc, const GhostCell* gl, long long n, u16* fg, u16* gg,
                         cudaStream_t s);
     static void coalesce(const LowpK* kc, const LowpK* kf, const CoalesceCell* cl, long long n, u16* fo, u16* go,

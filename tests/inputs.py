@@ -125,7 +125,7 @@ def gaussian_field(n, seed, corr=8.0):
     ky = np.fft.fftfreq(n[1])[None, :, None] * 2 * np.pi
     kx = np.fft.rfftfreq(n[0])[None, None, :] * 2 * np.pi
     filt = np.exp(-(kx ** 2 + ky ** 2 + kz ** 2) * corr ** 2 / 2)
-    gfield = np.fft.irfftn(np.fft.rfftn(w) * filt, s=w.shape)
+    gfield = np.fft.irfftn(np.fft.rfftn(w) * filt, s=w.shape, axes=(0, 1, 2))
     gfield -= gfield.mean()
     gfield /= gfield.std()
     return gfield.reshape(-1)

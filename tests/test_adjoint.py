@@ -47,17 +47,22 @@ def test_adjoint_matches_finite_differences():
     L0, Tf = loss(T0)
     grad = adj.backward(Tf - Tt)
     assert np.isfinite(grad).all() and np.abs(grad).max() > 0
+    # Errors are relative to the directional derivative, floored at 1e-3 of
+    # |grad| (a random direction can be nearly orthogonal to the gradient,
+    # where the difference quotient's round-off, ~1e-11 here, would dominate).
     rng = np.random.default_rng(5)
-    eps = 1e-6
-    worst = 0.0
+    gnorm = float(np.linalg.norm(grad))
+    worst = {1e-6: 0.0, 1e-5: 0.0}
     for _ in range(16):
         d = rng.standard_normal(T0.size)
         d /= np.linalg.norm(d)
-        fd = (loss(T0 + eps * d)[0] - loss(T0 - eps * d)[0]) / (2 * eps)
         ad = float(grad @ d)
-        worst = max(worst, abs(fd - ad) / max(abs(fd), 1e-300))
+        for eps in worst:
+            fd = (loss(T0 + eps * d)[0] - loss(T0 - eps * d)[0]) / (2 * eps)
+            worst[eps] = max(worst[eps], abs(fd - ad) / max(abs(fd), 1e-3 * gnorm))
     print("adjoint vs central differences: worst relative error", worst)
-    assert worst < 1e-6
+    assert worst[1e-6] < 1e-6
+    assert worst[1e-5] < 1e-7
 
 
 def test_checkpoint_interval_does_not_change_the_gradient():

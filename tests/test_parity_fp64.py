@@ -189,3 +189,27 @@ def test_drop_in_driver_matches_oracle():
     d.evolve(6)
     o.step(6)
     _compare(ctx, o, len(levels))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_graph_replay_equals_eager_steps(prec):
+    """mbg_step(n) replays a captured graph of two coarse steps; the state
+    must equal that of n steps launched one by one, bit for bit."""
+    import marbles_gb300 as M
+    p, levels = cases.gaussian_pulse(nc=32, fine_lo=8, fine_hi=23, mgs=16, width=3.0, t0=0.1)
+    o = cases.run_oracle(p, levels, 0)
+    ctxs = []
+    for _ in range(2):
+        c = M.Context(cases.mbg_params_from(p, prec))
+        for lev, b in enumerate(levels):
+            c.define_level(lev, b, o.get_grown_flags(lev))
+            f, g = o.get_state(lev)
+            c.set_state(lev, f, g)
+        ctxs.append(c)
+    ctxs[0].step(7)            # one eager step, then graph replays, then one eager step
+    for _ in range(7):
+        ctxs[1].step(1)
+    for lev in range(len(levels)):
+        fa, ga = ctxs[0].get_state(lev)
+        fb, gb = ctxs[1].get_state(lev)
+        assert np.array_equal(fa, fb) and np.array_equal(ga, gb)
