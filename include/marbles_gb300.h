@@ -233,8 +233,8 @@ void mbg_batch_destroy(mbg_batch* b);
  * field (of the stored populations).  mbg_adj_backward takes dL/dT_final of
  * the last forward run and returns dL/dT0: the hand-written discrete adjoint
  * of every step, walked backwards segment by segment, each segment recomputed
- * from its checkpoint; FP64 throughout.  Memory: about (2 + nsteps/K + K)
- * states of 432 bytes per cell. */
+ * from its checkpoint; FP64 throughout.  Memory: about (3 + nsteps/K + K)
+ * states of 432 bytes per cell plus K x 136 bytes per cell. */
 typedef struct mbg_adj mbg_adj;
 mbg_status mbg_adj_create(const mbg_params* p, double rho0, const double u0[3], void* cuda_stream, mbg_adj** out);
 mbg_status mbg_adj_forward(mbg_adj* a, const double* T0, int nsteps, int K, double* T_final);

@@ -13,7 +13,7 @@
 //
 // Reverse.  With s' = C(P(s)) (P the periodic pull, C the per-cell
 // collision, which couples neighbours only through dQ), one reverse step is
-// (Q_corr of the step's input state kept from the segment's recomputation)
+// (the step's moment sums and dQ kept from the segment's recomputation)
 //   k_adj_a1 : per cell, the transpose of the collision's Jacobian applied to
 //              the adjoint of the step's output: adjoints of the 14 moment
 //              sums reached through the macro fields, omega and the
@@ -332,16 +332,26 @@ __global__ void k_adj_q(AdjBox b, Phys64 ph, const double* f, const double* g, d
     Q[2 * b.N + c] = m.qcz;
 }
 
+// fields a reverse step reads from its forward step: the 14 moment sums of
+// the pulled values and dQ (component-major [k][N])
+enum { MOM_N = 17 };
+
 __global__ void k_adj_step(AdjBox b, Phys64 ph, const double* f, const double* g, const double* Q, double* fo,
-                           double* go)
+                           double* go, double* mom)
 {
     int x, y, z;
     long long c;
     if (!adj_cell(b, x, y, z, c)) return;
-    const Macro<double> m = pulled_moments(b, x, y, z, f, g, nullptr, nullptr).finish(ph.mesh_speed, ph.Rg, ph.cv);
+    const MomentAcc<double> acc = pulled_moments(b, x, y, z, f, g, nullptr, nullptr);
+    const Macro<double> m = acc.finish(ph.mesh_speed, ph.Rg, ph.cv);
     const double dqx = dq_axis(b, Q, x, y, z, 0, ph.idx[0]);
     const double dqy = dq_axis(b, Q, x, y, z, 1, ph.idx[1]);
     const double dqz = dq_axis(b, Q, x, y, z, 2, ph.idx[2]);
+    if (mom) {
+        const double v[MOM_N] = {acc.rho, acc.u, acc.v, acc.w, acc.pxx, acc.pyy, acc.pzz, acc.pxy, acc.pxz,
+                                 acc.pyz, acc.tre, acc.qx, acc.qy, acc.qz, dqx, dqy, dqz};
+        for (int k = 0; k < MOM_N; ++k) mom[k * b.N + c] = v[k];
+    }
     Equilibrium<double> E;
     const double omega = build_equilibrium<double>(m, dqx, dqy, dqz, ph.nu, ph.alpha, ph.dt, ph.Rg, ph.cv, ph.lat, E);
 #define MBG_AS(q)                                                                                       \
@@ -476,14 +486,27 @@ __global__ void k_adj_seed(AdjBox b, Phys64 ph, const double* f, const double* g
 
 // ---- reverse kernels -----------------------------------------------------
 __global__ void __launch_bounds__(128) k_adj_a1(AdjBox b, Phys64 ph, const double* f, const double* g,
-                                                const double* Q, const double* lf, const double* lg, double* ws)
+                                                const double* mom, const double* lf, const double* lg, double* ws)
 {
     int x, y, z;
     long long c;
     if (!adj_cell(b, x, y, z, c)) return;
-    const MomentAcc<double> acc = pulled_moments(b, x, y, z, f, g, nullptr, nullptr);
-    const double dq[3] = {dq_axis(b, Q, x, y, z, 0, ph.idx[0]), dq_axis(b, Q, x, y, z, 1, ph.idx[1]),
-                          dq_axis(b, Q, x, y, z, 2, ph.idx[2])};
+    MomentAcc<double> acc;
+    acc.rho = mom[c];
+    acc.u = mom[b.N + c];
+    acc.v = mom[2 * b.N + c];
+    acc.w = mom[3 * b.N + c];
+    acc.pxx = mom[4 * b.N + c];
+    acc.pyy = mom[5 * b.N + c];
+    acc.pzz = mom[6 * b.N + c];
+    acc.pxy = mom[7 * b.N + c];
+    acc.pxz = mom[8 * b.N + c];
+    acc.pyz = mom[9 * b.N + c];
+    acc.tre = mom[10 * b.N + c];
+    acc.qx = mom[11 * b.N + c];
+    acc.qy = mom[12 * b.N + c];
+    acc.qz = mom[13 * b.N + c];
+    const double dq[3] = {mom[14 * b.N + c], mom[15 * b.N + c], mom[16 * b.N + c]};
     double la[14], ldq[3], omega;
     collide_reverse(acc, dq, ph, CellPull{&b, x, y, z, f, g}, lf + c, lg + c, b.N, la, ldq, omega);
     for (int i = 0; i < 14; ++i) ws[(WS_LA + i) * b.N + c] = la[i];
@@ -582,7 +605,8 @@ struct mbg_adj {
     double *T0 = nullptr, *Tx = nullptr;
     std::vector<double*> ckpt;    // checkpoints, [f | g] each
     std::vector<double*> seg;     // states of the segment being reversed
-    std::vector<double*> segq;    // their Q_corr (computed by the recomputation)
+    std::vector<double*> segm;    // their forward moments and dQ (MOM_N fields)
+    double* tmpo = nullptr;       // throw-away output of the last state's forward step
     int cur = 0;
     int nsteps = -1, K = 0;
     long long launches = 0;
@@ -613,11 +637,10 @@ static mbg_status aalloc(mbg_adj* a, double** p, size_t count)
 
 static unsigned nblk(const mbg_adj* a) { return (unsigned)((a->b.N + 127) / 128); }
 
-static void fwd_step(mbg_adj* a, const double* f, const double* g, double* fo, double* go, double* Q = nullptr)
+static void fwd_step(mbg_adj* a, const double* f, const double* g, double* fo, double* go, double* mom = nullptr)
 {
-    if (!Q) Q = a->Q;
-    k_adj_q<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, Q);
-    k_adj_step<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, Q, fo, go);
+    k_adj_q<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, a->Q);
+    k_adj_step<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, a->Q, fo, go, mom);
     a->launches += 2;
 }
 
@@ -730,12 +753,16 @@ mbg_status mbg_adj_backward(mbg_adj* a, const double* dL_dTfinal, double* dL_dT0
     const int K = a->K, nsteps = a->nsteps;
     // segment states
     while ((int)a->seg.size() < K) {
-        double *c = nullptr, *cq = nullptr;
+        double *c = nullptr, *cm = nullptr;
         mbg_status st = aalloc(a, &c, 2 * N * NQ);
-        if (st == MBG_OK) st = aalloc(a, &cq, 3 * N);
+        if (st == MBG_OK) st = aalloc(a, &cm, (size_t)MOM_N * N);
         if (st != MBG_OK) return st;
         a->seg.push_back(c);
-        a->segq.push_back(cq);
+        a->segm.push_back(cm);
+    }
+    if (!a->tmpo) {
+        mbg_status st = aalloc(a, &a->tmpo, 2 * N * NQ);
+        if (st != MBG_OK) return st;
     }
     // adjoint of the final state from dL/dT_final
     ACUDA(cudaMemcpyAsync(a->Tx, dL_dTfinal, N * sizeof(double), cudaMemcpyHostToDevice, a->s));
@@ -747,18 +774,18 @@ mbg_status mbg_adj_backward(mbg_adj* a, const double* dL_dTfinal, double* dL_dT0
         const int n0 = ci * K, n1 = std::min(nsteps, n0 + K);
         // recompute the segment's states from its checkpoint
         ACUDA(cudaMemcpyAsync(a->seg[0], a->ckpt[ci], 2 * N * NQ * sizeof(double), cudaMemcpyDeviceToDevice, a->s));
-        // (with the Q_corr of every state, which the reverse steps reuse)
+        // (keeping each step's moments and dQ, which the reverse steps read;
+        // the last state's step runs into a throw-away output for them)
         for (int i = 1; i < n1 - n0; ++i)
-            fwd_step(a, a->seg[i - 1], a->seg[i - 1] + N * NQ, a->seg[i], a->seg[i] + N * NQ, a->segq[i - 1]);
+            fwd_step(a, a->seg[i - 1], a->seg[i - 1] + N * NQ, a->seg[i], a->seg[i] + N * NQ, a->segm[i - 1]);
         {
             const double* fl = a->seg[n1 - n0 - 1];
-            k_adj_q<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, fl, fl + N * NQ, a->segq[n1 - n0 - 1]);
-            a->launches++;
+            fwd_step(a, fl, fl + N * NQ, a->tmpo, a->tmpo + N * NQ, a->segm[n1 - n0 - 1]);
         }
         for (int n = n1 - 1; n >= n0; --n) {
             const double* f = a->seg[n - n0];
             const double* g = f + N * NQ;
-            k_adj_a1<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, a->segq[n - n0], a->lf[lc], a->lg[lc], a->ws);
+            k_adj_a1<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, f, g, a->segm[n - n0], a->lf[lc], a->lg[lc], a->ws);
             k_adj_a2<<<nblk(a), 128, 0, a->s>>>(a->b, a->ph, a->ws, a->lf[lc], a->lg[lc], a->lf[1 - lc],
                                                  a->lg[1 - lc]);
             a->launches += 2;

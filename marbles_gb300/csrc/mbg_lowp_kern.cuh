@@ -737,9 +737,7 @@ __global__ void k_ghost_general16(const LowpK* __restrict__ K, const GhostCell* 
 }
 
 // explosion (conservative linear interpolation, as in mbg_fp64_amr.cu) in
-// FP32: one warp per fine ghost cell, lane q interpolating direction q, the
-// limiter factor of each axis the minimum over the 27 components (blocks of
-// four warps)
+// FP32, the limiter factor of each axis the minimum over the 27 components
 template <bool BF>
 __device__ __forceinline__ long long crse16_index(const LV16& C, const int p0[3], int d, int s_)
 {
@@ -756,13 +754,13 @@ template <bool BF>
 __global__ void k_explode16(const LowpK* __restrict__ KF, const LowpK* __restrict__ KC, const GhostCell* gl,
                             long long n, u16* fg, u16* gg)
 {
-    const long long e = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int q = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const bool act = e < n && q < NQ;
-    __shared__ float sa[4][3][32];   // per warp: limiter candidates of each axis and direction
+    // one thread per fine ghost cell: neighbouring threads read neighbouring
+    // coarse cells, so every component's loads coalesce
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
     const LV16& F = KF->L;
     const LV16& C = KC->L;
-    const GhostCell g = gl[e < n ? e : 0];
+    const GhostCell g = gl[e];
     const DevBox& B = F.box[g.box];
     int fp[3] = {B.lo[0] + g.x, B.lo[1] + g.y, B.lo[2] + g.z};
     wrap_pos(F, fp);
@@ -779,30 +777,27 @@ __global__ void k_explode16(const LowpK* __restrict__ KF, const LowpK* __restric
     for (int lat = 0; lat < 2; ++lat) {
         const bool isg = lat == 1;
         const u16* v = isg ? KC->s.g : KC->s.f;
-        float u[7];
-        for (int k = 0; k < 7; ++k) u[k] = (act && ix[k] >= 0) ? dec<BF>(KC->ct, v[q * C.N + ix[k]], q, isg) : 0.0f;
-        float alpha[3], c[3];
-        for (int d = 0; d < 3; ++d) {
-            const float um = u[1 + 2 * d], up = u[2 + 2 * d], u0 = u[0];
-            const float cen = 0.5f * (up - um);
-            const float forw = 2.0f * (up - u0);
-            const float back = 2.0f * (u0 - um);
-            const float slp = (forw * back >= 0.f) ? fminf(fabsf(forw), fabsf(back)) : 0.f;
-            float a = (act && cen != 0.f) ? fminf(slp, fabsf(cen)) / fabsf(cen) : 1.0f;
-            sa[w][d][q] = a;
-            c[d] = cen;
+        u16* out = isg ? gg : fg;
+        auto at = [&](int k, int q) { return ix[k] >= 0 ? dec<BF>(KC->ct, v[q * C.N + ix[k]], q, isg) : 0.0f; };
+        float alpha[3] = {1.f, 1.f, 1.f};
+        for (int d = 0; d < 3; ++d)
+            for (int q = 0; q < NQ; ++q) {
+                const float u0 = at(0, q), um = at(1 + 2 * d, q), up = at(2 + 2 * d, q);
+                const float cen = 0.5f * (up - um);
+                const float forw = 2.0f * (up - u0);
+                const float back = 2.0f * (u0 - um);
+                const float slp = (forw * back >= 0.f) ? fminf(fabsf(forw), fabsf(back)) : 0.f;
+                if (cen != 0.f) alpha[d] = fminf(alpha[d], fminf(slp, fabsf(cen)) / fabsf(cen));
+            }
+        for (int q = 0; q < NQ; ++q) {
+            const float u0 = at(0, q);
+            const float cx = 0.5f * (at(2, q) - at(1, q));
+            const float cy = 0.5f * (at(4, q) - at(3, q));
+            const float cz = 0.5f * (at(6, q) - at(5, q));
+            out[q * F.NG + gi] =
+                enc<BF>(KF->ct, u0 + off[0] * (alpha[0] * cx) + off[1] * (alpha[1] * cy) + off[2] * (alpha[2] * cz),
+                        q, isg);
         }
-        __syncwarp();
-        for (int d = 0; d < 3; ++d) {
-            float a = 1.0f;
-            for (int l = 0; l < NQ; ++l) a = fminf(a, sa[w][d][l]);
-            alpha[d] = a;
-        }
-        __syncwarp();
-        if (act)
-            (isg ? gg : fg)[q * F.NG + gi] = enc<BF>(
-                KF->ct, u[0] + off[0] * (alpha[0] * c[0]) + off[1] * (alpha[1] * c[1]) + off[2] * (alpha[2] * c[2]),
-                q, isg);
     }
 }
 
@@ -977,7 +972,7 @@ template <bool BF>
 void Lowp16<BF>::explode(const LowpK* kf, const LowpK* kc, const GhostCell* gl, long long n, u16* fg, u16* gg,
                          cudaStream_t s)
 {
-    if (n > 0) k_explode16<BF><<<(unsigned)((n * 32 + 127) / 128), 128, 0, s>>>(kf, kc, gl, n, fg, gg);
+    if (n > 0) k_explode16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(kf, kc, gl, n, fg, gg);
 }
 template <bool BF>
 void Lowp16<BF>::coalesce(const LowpK* kc, const LowpK* kf, const CoalesceCell* cl, long long n, u16* fo, u16* go,
