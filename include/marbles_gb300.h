@@ -153,6 +153,13 @@ mbg_status mbg_average_down(mbg_ctx* ctx, int crse_lev, int crse_ng);
  * LBM::compute_eb_forces (Source/LBM.cpp:994-1044). */
 mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3]);
 
+/* Conserved totals of the stored state over all levels, each cell counted on
+ * the finest level that holds it and weighted by its volume, accumulated in
+ * FP64 on the device (both forms): out = {mass, momentum x, y, z, sum of
+ * 2 rho E}.  No counterpart in the reference (its only global reduction is
+ * the EB-force sum, Source/LBM.cpp:1040); one reduction launch per level. */
+mbg_status mbg_conserved(mbg_ctx* ctx, double out[5]);
+
 /* Wait for all work queued on the context's stream; reports a latched
  * device-side error. */
 mbg_status mbg_synchronize(mbg_ctx* ctx);

@@ -117,6 +117,7 @@ def lib():
         L.mbg_batch_destroy.restype = None
         L.mbg_tuning.argtypes = [vp, C.c_int, C.POINTER(C.c_int), dp]
         L.mbg_eb_forces.argtypes = [vp, dp]
+        L.mbg_conserved.argtypes = [vp, dp]
         L.mbg_synchronize.argtypes = [vp]
         L.mbg_launch_count.argtypes = [vp]
         L.mbg_launch_count.restype = C.c_longlong
@@ -249,6 +250,12 @@ class Context:
         ms = np.zeros(4)
         self._check(self.L.mbg_tuning(self.h, lev, C.byref(v), _dp(ms)), "mbg_tuning")
         return v.value, ms.tolist()
+
+    def conserved(self):
+        """[mass, momentum x, y, z, sum of 2 rho E] over the hierarchy (FP64)."""
+        out = np.zeros(5)
+        self._check(self.L.mbg_conserved(self.h, _dp(out)), "mbg_conserved")
+        return out
 
     def eb_forces(self):
         out = np.zeros(3)

@@ -931,6 +931,23 @@ mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3])
     return MBG_OK;
 }
 
+mbg_status mbg_conserved(mbg_ctx* ctx, double out[5])
+{
+    if (!ctx || !out) return MBG_EINVAL;
+    if (ctx->lv.empty()) return fail(ctx, MBG_ESTATE, "mbg_conserved: no level defined");
+    MBG_CUDA(cudaMemsetAsync(ctx->d_red, 0, 5 * sizeof(double), ctx->s));
+    for (auto& L : ctx->lv) {
+        const double dV = L.dx[0] * L.dx[1] * L.dx[2];
+        if (ctx->p.precision != MBG_FP64) lowp_conserved(L.lowp, L.plan, dV, ctx->d_red, ctx->s);
+        else launch_conserved(L.plan, phys64(ctx, L), L.f[L.cur], L.g[L.cur], dV, ctx->d_red, ctx->s);
+        ctx->launches++;
+    }
+    MBG_CUDA(cudaGetLastError());
+    MBG_CUDA(cudaMemcpyAsync(out, ctx->d_red, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
 void* mbg_stream(const mbg_ctx* ctx) { return ctx ? (void*)ctx->s : nullptr; }
 
 mbg_status mbg_set_timing(mbg_ctx* ctx, int enable)

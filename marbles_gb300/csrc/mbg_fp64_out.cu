@@ -66,11 +66,56 @@ __global__ void k_eb_forces(LV L, const Tile* tiles, const double* f, const doub
         if (fs[d] != 0.0) atomicAdd(&out3[d], fs[d]);
 }
 
+
+// ---- conserved totals (FP64): mass, momentum, 2 rho E of the stored state ----
+// over fluid cells not covered by a finer level, weighted by the cell volume;
+// a shared-memory tree per block, one FP64 atomic per block and total
+__global__ void __launch_bounds__(TILE_CELLS) k_conserved(LV L, Phys64 ph, const Tile* tiles, const double* f,
+                                                          const double* g, double dV, double* out5)
+{
+    __shared__ double red[5][TILE_CELLS];
+    int b, x, y, z;
+    long long c;
+    double v[5] = {0, 0, 0, 0, 0};
+    if (cell_of_tile(L, tiles, b, x, y, z, c)) {
+        const DevBox& B = L.box[b];
+        const uint8_t tf = flag_at(L, B, x, y, z);
+        if ((tf & FL_FLUID) && !(tf & FL_COV)) {
+            const long long cell = B.voff + c;
+            MomentAcc<double> acc;
+#define MBG_CN64(q) acc.template add<q>(f[q * L.N + cell], g[q * L.N + cell]);
+            MBG_UNROLL27(MBG_CN64)
+#undef MBG_CN64
+            v[0] = acc.rho * dV;
+            v[1] = acc.u * ph.mesh_speed * dV;
+            v[2] = acc.v * ph.mesh_speed * dV;
+            v[3] = acc.w * ph.mesh_speed * dV;
+            v[4] = acc.tre * dV;
+        }
+    }
+    const int t = threadIdx.x;
+    for (int k = 0; k < 5; ++k) red[k][t] = v[k];
+    __syncthreads();
+    for (int h = TILE_CELLS / 2; h > 0; h >>= 1) {
+        if (t < h)
+            for (int k = 0; k < 5; ++k) red[k][t] += red[k][t + h];
+        __syncthreads();
+    }
+    if (t == 0)
+        for (int k = 0; k < 5; ++k) atomicAdd(&out5[k], red[k][0]);
+}
+
 void launch_macro_local(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, double* out19,
                         cudaStream_t s)
 {
     if (lp.ntiles == 0) return;
     k_macro_local<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, ph, lp.tiles, f, g, out19);
+}
+
+void launch_conserved(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, double dV, double* out5,
+                      cudaStream_t s)
+{
+    if (lp.ntiles > 0) k_conserved<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, ph, lp.tiles, f, g, dV, out5);
 }
 
 void launch_eb_forces(const LevelPlan& lp, const double* f, const double* fg, double* out3, cudaStream_t s)

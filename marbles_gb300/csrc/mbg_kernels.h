@@ -84,5 +84,7 @@ void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParam
 void launch_macro_local(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, double* out19,
                         cudaStream_t s);
 void launch_eb_forces(const LevelPlan& lp, const double* f, const double* fg, double* out3, cudaStream_t s);
+void launch_conserved(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, double dV, double* out5,
+                      cudaStream_t s);
 
 }  // namespace mbg

@@ -502,6 +502,13 @@ mbg_status lowp_macro(LowpLevel& L, const LevelPlan& plan, double* out19, cudaSt
     return MBG_OK;
 }
 
+void lowp_conserved(LowpLevel& L, const LevelPlan& plan, double dV, double* out5, cudaStream_t s)
+{
+    LowpDev* D = dev_of(L);
+    ensure_k(L, plan, known_bc(L), D->with_override, s);
+    LOWP16(L.precision == MBG_FP32C_BF16S, conserved, D->dk + L.cur, plan.tiles, plan.ntiles, dV, out5, s);
+}
+
 int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const LevelPlan& plan, double dt,
                  const double idx[3], const CoalesceCell* coal, long long ncoal, const LowpLevel* fine,
                  const LevelPlan* fplan, cudaStream_t s, const LowpRunner& run)

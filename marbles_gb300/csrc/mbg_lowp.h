@@ -43,6 +43,8 @@ mbg_status lowp_set_state(LowpLevel& L, const LevelPlan& plan, const std::vector
 mbg_status lowp_get_state(LowpLevel& L, const LevelPlan& plan, const std::vector<DevBox>& hbox, double* f,
                           double* g, cudaStream_t s, std::string& err);
 mbg_status lowp_macro(LowpLevel& L, const LevelPlan& plan, double* out19, cudaStream_t s, std::string& err);
+// adds the level's conserved totals (FP64) to out5 on the device
+void lowp_conserved(LowpLevel& L, const LevelPlan& plan, double dV, double* out5, cudaStream_t s);
 // Stages of one 16-bit level advance, each one kernel launch; the caller's
 // runner wraps every launch (the library times them with CUDA events).
 enum { LOWP_STAGE_COALESCE = 0, LOWP_STAGE_GHOST_STREAM, LOWP_STAGE_FUSED, LOWP_STAGE_HALO };

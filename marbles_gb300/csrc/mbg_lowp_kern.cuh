@@ -846,8 +846,12 @@ __global__ void k_coalesce16(const LowpK* __restrict__ KC, const LowpK* __restri
                         dec<BF>(KF->ct, fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg), q, isg);
                     if (fabsf(fv + 1.0f) > small_num) { sum += (double)fv; ++vol; }
                 }
+        // 1 / vol for vol = 1..8 (the result is rounded to FP32 and then to
+        // 16 bits, so a product with the rounded reciprocal is as good as
+        // the FP64 division)
+        constexpr double inv[9] = {0.0, 1.0, 0.5, 1.0 / 3.0, 0.25, 0.2, 1.0 / 6.0, 1.0 / 7.0, 0.125};
         u16 r;
-        if (vol > 0) r = enc<BF>(KC->ct, (float)(sum / (double)vol), q, isg);
+        if (vol > 0) r = enc<BF>(KC->ct, (float)(sum * inv[vol]), q, isg);
         else if (into_state) r = (isg ? KC->s.g : KC->s.f)[q * C.N + cell];
         else r = enc<BF>(KC->ct, pull16_rt<BF>(q, KC, cc.cbox, cc.cx, cc.cy, cc.cz, flag_at(C, O, cc.cx, cc.cy, cc.cz),
                                                isg ? 1 : 0), q, isg);
@@ -916,6 +920,48 @@ __global__ void k_macro16(const LowpK* __restrict__ K, const CodecTab ct, const 
                              m.qcx, m.qcy, m.qcz, m.pxx, m.pyy, m.pzz, m.pxy, m.pxz, m.pyz,
                              m.qx, m.qy, m.qz, m.temp};
     for (int k = 0; k < 19; ++k) o[k * vol] = vals[k];
+}
+
+// conserved totals of the decoded stored state, FP64 accumulation (as
+// mbg_fp64_out.cu::k_conserved)
+template <bool BF>
+__global__ void __launch_bounds__(TILE_CELLS) k_conserved16(const LowpK* __restrict__ K, const Tile* tiles, double dV,
+                                                            double* out5)
+{
+    __shared__ double red[5][TILE_CELLS];
+    const LV16& L = K->L;
+    const Tile t0 = tiles[blockIdx.x];
+    const DevBox& B = L.box[t0.box];
+    int x, y, z;
+    double v[5] = {0, 0, 0, 0, 0};
+    if (tile_cell(B, t0, x, y, z)) {
+        const uint8_t tf = flag_at(L, B, x, y, z);
+        if ((tf & FL_FLUID) && !(tf & FL_COV)) {
+            const long long cell = B.voff + val_lin(B, x, y, z);
+            MomentAcc<double> acc;
+#define MBG_CN16(q)                                                                                     \
+    acc.template add<q>((double)dec<BF>(K->ct, K->s.f[q * L.N + cell], q, false),                       \
+                        (double)dec<BF>(K->ct, K->s.g[q * L.N + cell], q, true));
+            MBG_UNROLL27(MBG_CN16)
+#undef MBG_CN16
+            const double ms = K->ph.mesh_speed;
+            v[0] = acc.rho * dV;
+            v[1] = acc.u * ms * dV;
+            v[2] = acc.v * ms * dV;
+            v[3] = acc.w * ms * dV;
+            v[4] = acc.tre * dV;
+        }
+    }
+    const int t = threadIdx.x;
+    for (int k = 0; k < 5; ++k) red[k][t] = v[k];
+    __syncthreads();
+    for (int h = TILE_CELLS / 2; h > 0; h >>= 1) {
+        if (t < h)
+            for (int k = 0; k < 5; ++k) red[k][t] += red[k][t + h];
+        __syncthreads();
+    }
+    if (t == 0)
+        for (int k = 0; k < 5; ++k) atomicAdd(&out5[k], red[k][0]);
 }
 
 // ---- launchers ---------------------------------------------------------------
@@ -992,6 +1038,11 @@ void Lowp16<BF>::decode(const LowpK* k, const Tile* tiles, int ntiles, const u16
                         int isg, cudaStream_t s)
 {
     if (ntiles > 0) k_decode16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, tiles, src, NV, dst, isg);
+}
+template <bool BF>
+void Lowp16<BF>::conserved(const LowpK* k, const Tile* tiles, int ntiles, double dV, double* out5, cudaStream_t s)
+{
+    if (ntiles > 0) k_conserved16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, tiles, dV, out5);
 }
 template <bool BF>
 void Lowp16<BF>::macro(const LowpK* k, const CodecTab& ct, const Tile* tiles, int ntiles, double* out19,

@@ -85,6 +85,7 @@ struct Lowp16 {
                        int isg, cudaStream_t s);
     static void macro(const LowpK* k, const CodecTab& ct, const Tile* tiles, int ntiles, double* out19,
                       cudaStream_t s);
+    static void conserved(const LowpK* k, const Tile* tiles, int ntiles, double dV, double* out5, cudaStream_t s);
 };
 extern template struct Lowp16<false>;
 extern template struct Lowp16<true>;

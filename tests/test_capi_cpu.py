@@ -60,3 +60,25 @@ def test_create_rejects_pressure_bc():
     p.bc_hi[:] = [5, 0, 0]
     with pytest.raises(M.MbgError, match="pressure"):
         M.Context(p)
+
+
+def test_batch_and_adjoint_reject_bad_parameters():
+    """Host-side validation of the batch and adjoint entry points (no GPU
+    work happens before these checks)."""
+    import math
+    import marbles_gb300 as M
+    p = M.default_params()
+    p.precision = 0            # the batch is a 16-bit form only
+    with pytest.raises(M.MbgError, match="16-bit"):
+        M.Batch(p, [([8, 8, 8], [0.0] * 3, [2 * math.pi] * 3, 0.1, 0.1)])
+    p.precision = 1
+    with pytest.raises(M.MbgError, match="invalid extent"):
+        M.Batch(p, [([1, 8, 8], [0.0] * 3, [2 * math.pi] * 3, 0.1, 0.1)])
+    q = M.default_params()
+    q.is_periodic[:] = [0, 1, 1]
+    with pytest.raises(M.MbgError, match="periodic"):
+        M.Adjoint(q)
+    q = M.default_params()
+    q.precision = 1
+    with pytest.raises(M.MbgError, match="FP64"):
+        M.Adjoint(q)
