@@ -846,12 +846,10 @@ __global__ void k_coalesce16(const LowpK* __restrict__ KC, const LowpK* __restri
                         dec<BF>(KF->ct, fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg), q, isg);
                     if (fabsf(fv + 1.0f) > small_num) { sum += (double)fv; ++vol; }
                 }
-        // 1 / vol for vol = 1..8 (the result is rounded to FP32 and then to
-        // 16 bits, so a product with the rounded reciprocal is as good as
-        // the FP64 division)
-        constexpr double inv[9] = {0.0, 1.0, 0.5, 1.0 / 3.0, 0.25, 0.2, 1.0 / 6.0, 1.0 / 7.0, 0.125};
+        // all eight children unmasked is the common case: sum / 8 is the
+        // exact product sum * 0.125, no FP64 division
         u16 r;
-        if (vol > 0) r = enc<BF>(KC->ct, (float)(sum * inv[vol]), q, isg);
+        if (vol > 0) r = enc<BF>(KC->ct, (float)(vol == 8 ? sum * 0.125 : sum / (double)vol), q, isg);
         else if (into_state) r = (isg ? KC->s.g : KC->s.f)[q * C.N + cell];
         else r = enc<BF>(KC->ct, pull16_rt<BF>(q, KC, cc.cbox, cc.cx, cc.cy, cc.cz, flag_at(C, O, cc.cx, cc.cy, cc.cz),
                                                isg ? 1 : 0), q, isg);
