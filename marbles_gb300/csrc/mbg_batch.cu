@@ -100,7 +100,8 @@ static void launch_step(mbg_batch* b, int cur)
     LOWP16(b->bf, halo_periodic, k, b->halo, b->nhalo, b->s);
     if (b->variant == 0) {
         // no pad of Q_corr: every domain face is one-sided
-        LOWP16(b->bf, two_pass, k, b->ct, b->lat, b->tiles, b->ntiles, b->halo, 0, b->qs, b->s);
+        const QPtrs qp = make_qptrs(b->f[cur], b->g[cur], b->f[1 - cur], b->g[1 - cur], b->N);
+        LOWP16(b->bf, two_pass, k, b->ct, b->lat, b->tiles, b->ntiles, b->halo, 0, b->qs, qp, b->s);
         b->launches += 4;
     } else {
         const int v = b->variant - 1;
@@ -171,6 +172,11 @@ mbg_status mbg_batch_create(const mbg_params* common, int ndom, const mbg_domain
     }
     b->NV = hoff;
     b->N = pad_boxes(b->hbox);
+    if (b->N >= (1LL << 31)) {
+        mbg_set_global_error("mbg_batch_create: more than 2^31 padded cells");
+        mbg_batch_destroy(b);
+        return MBG_EINVAL;
+    }
     const std::vector<HaloCell> halo = halo_cells(b->hbox);
     b->nhalo = (long long)halo.size();
     std::vector<Tile> tiles;

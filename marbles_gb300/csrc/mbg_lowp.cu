@@ -328,6 +328,10 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     std::vector<DevBox> box = hbox;
     for (size_t n = 0; n < box.size(); ++n) box[n].hoff = hbox[n].voff;
     L.N = pad_boxes(box);
+    if (L.N >= (1LL << 31)) {
+        err = "16-bit form: a level holds more than 2^31 padded cells";
+        return MBG_EINVAL;
+    }
     const std::vector<HaloCell> halo = halo_cells(box);
     std::vector<long long> gdst, gsrc;
     std::vector<HaloCell> general;
@@ -542,7 +546,10 @@ int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const Le
     }
     if (D->variant == 0) {
         run(LOWP_STAGE_FUSED,
-            [&] { LOWP16(bf, two_pass, k, D->ct, D->lat, plan.tiles, plan.ntiles, D->halo, D->nhalo, D->qs, s); });
+            [&] {
+                const QPtrs qp = make_qptrs(L.f[A], L.g[A], L.f[1 - A], L.g[1 - A], L.N);
+                LOWP16(bf, two_pass, k, D->ct, D->lat, plan.tiles, plan.ntiles, D->halo, D->nhalo, D->qs, qp, s);
+            });
         launches += 3;
     } else {
         const int v = D->variant - 1;

@@ -518,19 +518,26 @@ __device__ __forceinline__ bool present_vf(const LV16& L, const DevBox& B, int c
     return !(B.own_domain && (p < 0 || p >= B.n[d]));
 }
 
+// uniform pull through the per-direction base pointer (c: 32-bit storage
+// index of the target within one component)
+template <int q, bool BF>
+__device__ __forceinline__ float pullq(const CodecTab& ct, const u16* __restrict__ base, int c, int sy, int sz,
+                                       bool is_g)
+{
+    constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
+    return dec<BF>(ct, __ldg(base + (c - (ez * sz + ey * sy + ex))), q, is_g);
+}
+
 template <bool BF>
 __device__ __forceinline__ MomentAcc<float> moments_at(const LowpK* __restrict__ K, const CodecTab& ct,
-                                                       const DevBox& B, int b, int x, int y, int z, long long c,
-                                                       uint8_t tf)
+                                                       const QPtrs& qp, const DevBox& B, int b, int x, int y, int z,
+                                                       long long c, uint8_t tf)
 {
     MomentAcc<float> acc;
     if (B.vfluid && !((tf & FL_OVR) && K->s.fo)) {
-        const u16* __restrict__ sf = K->s.f;
-        const u16* __restrict__ sg = K->s.g;
-        const long long N = K->L.N;
-        const int sy = B.sy, sz = B.sz;
+        const int c32 = (int)c, sy = B.sy, sz = B.sz;
 #define MBG_MT16(q) \
-    acc.template add<q>(pullu<q, BF>(ct, sf, N, c, sy, sz, false), pullu<q, BF>(ct, sg, N, c, sy, sz, true));
+    acc.template add<q>(pullq<q, BF>(ct, qp.f[q], c32, sy, sz, false), pullq<q, BF>(ct, qp.g[q], c32, sy, sz, true));
         MBG_UNROLL27(MBG_MT16)
 #undef MBG_MT16
     } else {
@@ -541,7 +548,8 @@ __device__ __forceinline__ MomentAcc<float> moments_at(const LowpK* __restrict__
 
 template <bool BF>
 __global__ void __launch_bounds__(TILE_CELLS) k_qcorr16(const LowpK* __restrict__ K, const CodecTab ct,
-                                                        const Tile* __restrict__ tiles, float* __restrict__ qs)
+                                                        const Tile* __restrict__ tiles, float* __restrict__ qs,
+                                                        const QPtrs qp)
 {
     const LV16& L = K->L;
     const Tile t = tiles[blockIdx.x];
@@ -553,7 +561,7 @@ __global__ void __launch_bounds__(TILE_CELLS) k_qcorr16(const LowpK* __restrict_
     float qx = 0.f, qy = 0.f, qz = 0.f;
     if (tf & FL_FLUID) {
         const Macro<float> m =
-            moments_at<BF>(K, ct, B, t.box, x, y, z, c, tf).finish(K->ph.mesh_speed, K->ph.Rg, K->ph.cv);
+            moments_at<BF>(K, ct, qp, B, t.box, x, y, z, c, tf).finish(K->ph.mesh_speed, K->ph.Rg, K->ph.cv);
         qx = m.qcx;
         qy = m.qcy;
         qz = m.qcz;
@@ -605,7 +613,7 @@ __global__ void k_qhalo16(const LowpK* __restrict__ K, const HaloCell* __restric
 template <bool BF>
 __global__ void __launch_bounds__(TILE_CELLS, 5)
     k_collide16(const LowpK* __restrict__ K, const CodecTab ct, const Lattice<float> lat,
-                const Tile* __restrict__ tiles, const float* __restrict__ qs)
+                const Tile* __restrict__ tiles, const float* __restrict__ qs, const QPtrs qp)
 {
     const LV16& L = K->L;
     const Tile t = tiles[blockIdx.x];
@@ -632,7 +640,7 @@ __global__ void __launch_bounds__(TILE_CELLS, 5)
     }
     const Phys32* __restrict__ PH = K->phys ? K->phys + B.phys : &K->ph;
     const float Rg = K->ph.Rg, cv = K->ph.cv;
-    const Macro<float> m = moments_at<BF>(K, ct, B, t.box, x, y, z, c, tf).finish(K->ph.mesh_speed, Rg, cv);
+    const Macro<float> m = moments_at<BF>(K, ct, qp, B, t.box, x, y, z, c, tf).finish(K->ph.mesh_speed, Rg, cv);
     const int sy = B.sy, sz = B.sz;
     bool pr[6];
     if (B.vfluid) {
@@ -650,14 +658,13 @@ __global__ void __launch_bounds__(TILE_CELLS, 5)
     Equilibrium<float> E;
     const float omega = build_equilibrium<float>(m, dqx, dqy, dqz, PH->nu, PH->alpha, PH->dt, Rg, cv, lat, E);
     if (B.vfluid && !ovr) {
-        const u16* __restrict__ sf = K->s.f;
-        const u16* __restrict__ sg = K->s.g;
+        const int c32 = (int)c;
 #define MBG_RC16(q)                                                                                  \
     {                                                                                                \
-        const float fq = pullu<q, BF>(ct, sf, N, c, sy, sz, false);                                  \
-        fB[q * N + c] = enc<BF>(ct, fmaf(omega, E.template feq<q>() - fq, fq), q, false);            \
-        const float gq = pullu<q, BF>(ct, sg, N, c, sy, sz, true);                                   \
-        gB[q * N + c] = enc<BF>(ct, fmaf(omega, E.template geq<q>(lat) - gq, gq), q, true);          \
+        const float fq = pullq<q, BF>(ct, qp.f[q], c32, sy, sz, false);                              \
+        qp.fo[q][c32] = enc<BF>(ct, fmaf(omega, E.template feq<q>() - fq, fq), q, false);            \
+        const float gq = pullq<q, BF>(ct, qp.g[q], c32, sy, sz, true);                               \
+        qp.go[q][c32] = enc<BF>(ct, fmaf(omega, E.template geq<q>(lat) - gq, gq), q, true);          \
     }
         MBG_UNROLL27(MBG_RC16)
 #undef MBG_RC16
@@ -993,12 +1000,12 @@ int Lowp16<BF>::fused_blocks_per_sm()
 }
 template <bool BF>
 void Lowp16<BF>::two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
-                          int ntiles, const HaloCell* h, long long nh, float* qs, cudaStream_t s)
+                          int ntiles, const HaloCell* h, long long nh, float* qs, const QPtrs& qp, cudaStream_t s)
 {
     if (ntiles == 0) return;
-    k_qcorr16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, tiles, qs);
+    k_qcorr16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, tiles, qs, qp);
     if (nh > 0) k_qhalo16<BF><<<(unsigned)((nh + 127) / 128), 128, 0, s>>>(k, h, nh, qs);
-    k_collide16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs);
+    k_collide16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs, qp);
 }
 template <bool BF>
 void Lowp16<BF>::ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s)

@@ -59,6 +59,28 @@ long long pad_boxes(std::vector<DevBox>& box);
 std::vector<HaloCell> halo_cells(const std::vector<DevBox>& box);
 std::vector<FusedTile> fused_tiles(const std::vector<DevBox>& box, int zc);
 
+// per-direction base pointers of the source and destination arrays of one
+// step (kernel parameters, so each population access is one 32-bit offset
+// from a constant-bank operand)
+struct QPtrs {
+    const u16* f[NQ];
+    const u16* g[NQ];
+    u16* fo[NQ];
+    u16* go[NQ];
+};
+
+inline QPtrs make_qptrs(const void* f, const void* g, void* fo, void* go, long long N)
+{
+    QPtrs p;
+    for (int q = 0; q < NQ; ++q) {
+        p.f[q] = (const u16*)f + q * N;
+        p.g[q] = (const u16*)g + q * N;
+        p.fo[q] = (u16*)fo + q * N;
+        p.go[q] = (u16*)go + q * N;
+    }
+    return p;
+}
+
 // kernel launchers, instantiated for FP16 (BF = false) and BF16 (BF = true)
 template <bool BF>
 struct Lowp16 {
@@ -70,7 +92,7 @@ struct Lowp16 {
     static int fused_blocks_per_sm();   // resident CTAs of the fused step per SM
     // the two-pass step: Q_corr pass, pad of Q_corr, collision pass (3 launches)
     static void two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
-                         int ntiles, const HaloCell* h, long long nh, float* qs, cudaStream_t s);
+                         int ntiles, const HaloCell* h, long long nh, float* qs, const QPtrs& qp, cudaStream_t s);
     static void ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s);
     // the ghost stream through its plan: gather, then the general entries
     static void ghost_gather(const LowpK* k, const long long* dst, const long long* src, long long n,
