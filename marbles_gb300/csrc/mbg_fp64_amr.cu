@@ -107,17 +107,30 @@ __global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, const CoalesceCell
     const DevBox& A = F.box[cc.fbox];
     const long long cell = O.voff + val_lin(O, cc.cx, cc.cy, cc.cz);
     const double masked = -1.0;
+    const bool inA = cc.fx >= 0 && cc.fy >= 0 && cc.fz >= 0 && cc.fx + 1 < A.n[0] && cc.fy + 1 < A.n[1] &&
+                     cc.fz + 1 < A.n[2];
     for (int lat = 0; lat < 2; ++lat) {
         const double* v = lat ? gf : ff;
         const double* vg = lat ? gfg : ffg;
         const double* cA = lat ? gcA : fcA;
         double s = 0.0, vol = 0.0;
-        for (int kr = 0; kr < 2; ++kr)
-            for (int jr = 0; jr < 2; ++jr)
-                for (int ir = 0; ir < 2; ++ir) {
-                    const double fv = fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg);
-                    if (fabs(fv - masked) > ph.small_num) { s += fv; vol += 1.0; }
-                }
+        if (inA) {
+            // the eight children are valid cells of box A: fixed offsets
+            const double* c0 = v + (long long)q * F.N + A.voff + val_lin(A, cc.fx, cc.fy, cc.fz);
+            for (int kr = 0; kr < 2; ++kr)
+                for (int jr = 0; jr < 2; ++jr)
+                    for (int ir = 0; ir < 2; ++ir) {
+                        const double fv = c0[kr * A.sz + jr * A.sy + ir];
+                        if (fabs(fv - masked) > ph.small_num) { s += fv; vol += 1.0; }
+                    }
+        } else {
+            for (int kr = 0; kr < 2; ++kr)
+                for (int jr = 0; jr < 2; ++jr)
+                    for (int ir = 0; ir < 2; ++ir) {
+                        const double fv = fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg);
+                        if (fabs(fv - masked) > ph.small_num) { s += fv; vol += 1.0; }
+                    }
+        }
         double r;
         if (vol > 0.0) r = s / vol;
         else if (into_state) r = cA[q * C.N + cell];
