@@ -51,10 +51,14 @@ __global__ void k_explode(LV F, LV C, const GhostCell* gl, long long n, const do
         const double* v = lat ? gc_ : fc;
         double* out = lat ? gg : fg;
         auto at = [&](int k, int q) { return ix[k] >= 0 ? v[q * C.N + ix[k]] : 0.0; };
+        // limiter factors: directions outermost, the seven stencil values of
+        // each read once (fmin is exact, so the order of the minimum is free)
         double alpha[3] = {1.0, 1.0, 1.0};
-        for (int d = 0; d < 3; ++d) {
-            for (int q = 0; q < NQ; ++q) {
-                const double u0 = at(0, q), um = at(1 + 2 * d, q), up = at(2 + 2 * d, q);
+        for (int q = 0; q < NQ; ++q) {
+            double u[7];
+            for (int k = 0; k < 7; ++k) u[k] = at(k, q);
+            for (int d = 0; d < 3; ++d) {
+                const double u0 = u[0], um = u[1 + 2 * d], up = u[2 + 2 * d];
                 const double cen = 0.5 * (up - um);
                 const double forw = 2.0 * (up - u0);
                 const double back = 2.0 * (u0 - um);

@@ -787,15 +787,18 @@ __global__ void k_explode16(const LowpK* __restrict__ KF, const LowpK* __restric
         u16* out = isg ? gg : fg;
         auto at = [&](int k, int q) { return ix[k] >= 0 ? dec<BF>(KC->ct, v[q * C.N + ix[k]], q, isg) : 0.0f; };
         float alpha[3] = {1.f, 1.f, 1.f};
-        for (int d = 0; d < 3; ++d)
-            for (int q = 0; q < NQ; ++q) {
-                const float u0 = at(0, q), um = at(1 + 2 * d, q), up = at(2 + 2 * d, q);
+        for (int q = 0; q < NQ; ++q) {
+            float u[7];
+            for (int k = 0; k < 7; ++k) u[k] = at(k, q);
+            for (int d = 0; d < 3; ++d) {
+                const float u0 = u[0], um = u[1 + 2 * d], up = u[2 + 2 * d];
                 const float cen = 0.5f * (up - um);
                 const float forw = 2.0f * (up - u0);
                 const float back = 2.0f * (u0 - um);
                 const float slp = (forw * back >= 0.f) ? fminf(fabsf(forw), fabsf(back)) : 0.f;
                 if (cen != 0.f) alpha[d] = fminf(alpha[d], fminf(slp, fabsf(cen)) / fabsf(cen));
             }
+        }
         for (int q = 0; q < NQ; ++q) {
             const float u0 = at(0, q);
             const float cx = 0.5f * (at(2, q) - at(1, q));
