@@ -843,32 +843,19 @@ __global__ void k_coalesce16(const LowpK* __restrict__ KC, const LowpK* __restri
     const long long cell = O.voff + val_lin(O, cc.cx, cc.cy, cc.cz);
     // the mask test |v - (-1)| > SMALL_NUM on the FP32 decoded value; the sum in FP64
     const float small_num = (float)(2.220446049250313e-16 * 1e10);
-    const bool inA = cc.fx >= 0 && cc.fy >= 0 && cc.fz >= 0 && cc.fx + 1 < A.n[0] && cc.fy + 1 < A.n[1] &&
-                     cc.fz + 1 < A.n[2];
     for (int lat = 0; lat < 2; ++lat) {
         const bool isg = lat == 1;
         const u16* v = isg ? KF->s.g : KF->s.f;
         const u16* vg = isg ? KF->s.gg : KF->s.fg;
         double sum = 0.0;
         int vol = 0;
-        if (inA) {
-            // the eight children are valid cells of box A: fixed offsets
-            const u16* __restrict__ c0 = v + (long long)q * F.N + A.voff + val_lin(A, cc.fx, cc.fy, cc.fz);
-            for (int kr = 0; kr < 2; ++kr)
-                for (int jr = 0; jr < 2; ++jr)
-                    for (int ir = 0; ir < 2; ++ir) {
-                        const float fv = dec<BF>(KF->ct, c0[kr * A.sz + jr * A.sy + ir], q, isg);
-                        if (fabsf(fv + 1.0f) > small_num) { sum += (double)fv; ++vol; }
-                    }
-        } else {
-            for (int kr = 0; kr < 2; ++kr)
-                for (int jr = 0; jr < 2; ++jr)
-                    for (int ir = 0; ir < 2; ++ir) {
-                        const float fv =
-                            dec<BF>(KF->ct, fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg), q, isg);
-                        if (fabsf(fv + 1.0f) > small_num) { sum += (double)fv; ++vol; }
-                    }
-        }
+        for (int kr = 0; kr < 2; ++kr)
+            for (int jr = 0; jr < 2; ++jr)
+                for (int ir = 0; ir < 2; ++ir) {
+                    const float fv =
+                        dec<BF>(KF->ct, fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg), q, isg);
+                    if (fabsf(fv + 1.0f) > small_num) { sum += (double)fv; ++vol; }
+                }
         // all eight children unmasked is the common case: sum / 8 is the
         // exact product sum * 0.125, no FP64 division
         u16 r;
