@@ -90,3 +90,28 @@ def test_autograd_function():
     Tf = adj.forward(T0, 6, 3)
     ref = adj.backward(Tf - Tt)
     assert np.array_equal(t0.grad.numpy(), ref)
+
+
+def test_adjoint_matches_torch_tape():
+    """Reference gradient: autograd over an FP64 PyTorch restatement of the
+    same forward (tests/torch_tape.py).  The forward fields agree to
+    round-off and the gradients to 1e-9 of their largest entry."""
+    torch = pytest.importorskip("torch")
+    import marbles_gb300 as M
+    import torch_tape as TT
+    n = [6, 6, 8]
+    nsteps = 6
+    adj = M.Adjoint(_params(n))
+    T0, Tt = _fields(n, seed=21)
+    Tf = adj.forward(T0, nsteps, 4)
+    grad = adj.backward(Tf - Tt)
+    shape = (n[2], n[1], n[0])
+    t0 = torch.tensor(T0.reshape(shape), dtype=torch.float64, requires_grad=True)
+    tf = TT.final_temperature(t0, nsteps, TT.Params(nu=0.05, alpha=0.05))
+    loss = 0.5 * ((tf - torch.tensor(Tt.reshape(shape), dtype=torch.float64)) ** 2).sum()
+    loss.backward()
+    assert np.max(np.abs(tf.detach().numpy().reshape(-1) - Tf)) <= 1e-12 * np.max(np.abs(Tf))
+    gt = t0.grad.numpy().reshape(-1)
+    rel = float(np.max(np.abs(gt - grad)) / np.max(np.abs(gt)))
+    print("adjoint vs FP64 autograd tape: max relative difference", rel)
+    assert rel < 1e-9
