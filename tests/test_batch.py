@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 
 # u relative to each domain's largest velocity: the slowest domains (v0 down
 # to 0.01) keep fewer significant bits of u in the stored deviation
-TOL = {1: {"rho": 1e-4, "u": 3e-3, "T": 1e-4}, 2: {"rho": 1e-3, "u": 3e-2, "T": 1e-3}}
+TOL = {1: {"rho": 1e-4, "u": 3e-3, "T": 1e-4, "ke": 3e-3}, 2: {"rho": 1e-3, "u": 3e-2, "T": 1e-3, "ke": 3e-2}}
 
 
 def _setup(prec, count=6, seed0=7):
@@ -63,7 +63,7 @@ def test_batch_against_fp64(prec):
         r.step(20)
     a = b.get_macro()
     off = 0
-    worst = {"rho": 0.0, "u": 0.0, "T": 0.0}
+    worst = {"rho": 0.0, "u": 0.0, "T": 0.0, "ke": 0.0}
     for (n, _, _), r in zip(doms, ref):
         vol = int(np.prod(n))
         A = a[off * 19:(off + vol) * 19].reshape(19, vol)
@@ -72,6 +72,9 @@ def test_batch_against_fp64(prec):
         worst["rho"] = max(worst["rho"], float(np.max(np.abs(A[0] - R[0]) / R[0])))
         worst["T"] = max(worst["T"], float(np.max(np.abs(A[18] - R[18]) / R[18])))
         worst["u"] = max(worst["u"], float(np.max(np.abs(A[1:4] - R[1:4])) / np.max(np.abs(R[1:4]))))
+        ka = float(np.sum(0.5 * A[0] * (A[1:4] ** 2).sum(axis=0)))
+        kr = float(np.sum(0.5 * R[0] * (R[1:4] ** 2).sum(axis=0)))
+        worst["ke"] = max(worst["ke"], abs(ka - kr) / kr)   # kinetic energy of each domain
     print("batch form", prec, "errors", worst)
     assert all(worst[k] <= TOL[prec][k] for k in worst), worst
 

@@ -18,15 +18,18 @@ pytestmark = pytest.mark.gpu
 # FP16.  u is relative to the flow's largest velocity: 1e-3 for flows with a
 # mean velocity (Taylor-Green, inflow), looser for the acoustic pulse, whose
 # |u| ~ 1e-3 is only ~100 FP16 quanta of the deviation.
-TOL = {1: {"rho": 2.5e-4, "u": 1e-3, "T": 1e-3}, 2: {"rho": 2e-3, "u": 1e-2, "T": 2e-3}}
+TOL = {1: {"rho": 2.5e-4, "u": 1e-3, "T": 1e-3, "ke": 1e-3}, 2: {"rho": 2e-3, "u": 1e-2, "T": 2e-3, "ke": 1e-2}}
 TOL_PULSE_U = {1: 2e-2, 2: 1.5e-1}
+TOL_PULSE_KE = {1: 5e-2, 2: 3e-1}
 
 
-def _check(e, prec, u_tol=None):
+def _check(e, prec, u_tol=None, ke_tol=None):
     print("16-bit form", prec, "errors", e)
     tol = dict(TOL[prec])
     if u_tol is not None:
         tol["u"] = u_tol
+    if ke_tol is not None:
+        tol["ke"] = ke_tol
     assert all(e[k] <= tol[k] for k in e), (e, tol)
 
 
@@ -46,7 +49,11 @@ def _pair(p, levels, prec):
 
 
 def _errors(c64, c16, levels):
-    worst = {"rho": 0.0, "u": 0.0, "T": 0.0}
+    """Worst pointwise relative errors in rho and T, u relative to the
+    largest |u|, and the relative error of the kinetic energy
+    sum(rho |u|^2 / 2) over the hierarchy's fluid cells."""
+    worst = {"rho": 0.0, "u": 0.0, "T": 0.0, "ke": 0.0}
+    ke16 = ke64 = 0.0
     for lev in range(len(levels)):
         a = c16.get_macro(lev)
         r = c64.get_macro(lev)
@@ -62,6 +69,10 @@ def _errors(c64, c16, levels):
             worst["T"] = max(worst["T"], float(np.max(np.abs(A[18] - R[18])[fluid] / R[18][fluid])))
             umax = max(float(np.max(np.abs(R[1:4]))), 1e-30)
             worst["u"] = max(worst["u"], float(np.max(np.abs(A[1:4] - R[1:4]))) / umax)
+            dV = 8.0 ** -lev
+            ke16 += dV * float(np.sum(0.5 * A[0][fluid] * (A[1:4, fluid] ** 2).sum(axis=0)))
+            ke64 += dV * float(np.sum(0.5 * R[0][fluid] * (R[1:4, fluid] ** 2).sum(axis=0)))
+    worst["ke"] = abs(ke16 - ke64) / max(ke64, 1e-300)
     return worst
 
 
@@ -89,7 +100,7 @@ def test_two_level_pulse(prec):
     c64, c16 = _pair(p, levels, prec)
     c64.step(20)
     c16.step(20)
-    _check(_errors(c64, c16, levels), prec, TOL_PULSE_U[prec])
+    _check(_errors(c64, c16, levels), prec, TOL_PULSE_U[prec], TOL_PULSE_KE[prec])
 
 
 def test_three_level_sphere_fp16():
@@ -137,4 +148,4 @@ def test_autotune_keeps_state(prec):
         assert 0 <= v < 4 and all(t > 0 for t in ms)
     c64.step(18)
     c16.step(18)
-    _check(_errors(c64, c16, levels), prec, TOL_PULSE_U[prec])
+    _check(_errors(c64, c16, levels), prec, TOL_PULSE_U[prec], TOL_PULSE_KE[prec])
