@@ -181,8 +181,9 @@ mbg_status mbg_timing(mbg_ctx* ctx, int k, const char** name, long long* launche
 /* ---- autotuner ----------------------------------------------------------------
  * No counterpart in the reference.  The 16-bit forms have several
  * implementations of the level step: variant 0 runs it in two passes (Q_corr,
- * then collision), variants 1-3 fuse it into one pass over runs of 4, 8 or 16
- * planes per thread block.  mbg_autotune times every variant `reps` times on
+ * then collision), variants 1-2 fuse it into one pass over runs of 4 or 8
+ * planes per thread block, variant 3 is the two-pass step with the collision
+ * pass limited to 80 registers (6 resident blocks per SM).  mbg_autotune times every variant `reps` times on
  * each level's current data and keeps the fastest per level; the state is not
  * changed.  mbg_tuning reports a level's chosen variant and the mean time per
  * step of each variant in ms (0 where not timed).  FP64 contexts have one

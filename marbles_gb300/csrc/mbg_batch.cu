@@ -48,8 +48,8 @@ struct mbg_batch {
     long long nhalo = 0;
     Tile* tiles = nullptr;             // 128-cell tiles (two-pass variant, state transfer)
     int ntiles = 0;
-    FusedTile* ftiles[3] = {nullptr, nullptr, nullptr};
-    int nftiles[3] = {0, 0, 0};
+    FusedTile* ftiles[2] = {nullptr, nullptr};
+    int nftiles[2] = {0, 0};
     int fgrid = 0;                     // persistent grid of the fused variants
     LowpK hk[2];
     LowpK* dk = nullptr;
@@ -98,10 +98,10 @@ static void launch_step(mbg_batch* b, int cur)
 {
     const LowpK* k = b->dk + cur;
     LOWP16(b->bf, halo_periodic, k, b->halo, b->nhalo, b->s);
-    if (b->variant == 0) {
+    if (b->variant == 0 || b->variant == 3) {
         // no pad of Q_corr: every domain face is one-sided
         const QPtrs qp = make_qptrs(b->f[cur], b->g[cur], b->f[1 - cur], b->g[1 - cur], b->N);
-        LOWP16(b->bf, two_pass, k, b->ct, b->lat, b->tiles, b->ntiles, b->halo, 0, b->qs, qp, b->s);
+        LOWP16(b->bf, two_pass, k, b->ct, b->lat, b->tiles, b->ntiles, b->halo, 0, b->qs, qp, b->variant == 3, b->s);
         b->launches += 4;
     } else {
         const int v = b->variant - 1;
@@ -203,7 +203,7 @@ mbg_status mbg_batch_create(const mbg_params* common, int ndom, const mbg_domain
         if ((s2 = balloc(b, &b->d_phys, ndom)) != MBG_OK) return s2;
         if ((s2 = balloc(b, &b->halo, halo.size())) != MBG_OK) return s2;
         if ((s2 = balloc(b, &b->tiles, tiles.size())) != MBG_OK) return s2;
-        for (int v = 0; v < 3; ++v) {
+        for (int v = 0; v < 2; ++v) {
             std::vector<FusedTile> ft = fused_tiles(sorted, FUSED_ZC[v]);
             for (FusedTile& t : ft) t.box = order[t.box];
             b->nftiles[v] = (int)ft.size();

@@ -24,9 +24,9 @@ struct LowpDev {
     bool with_override = false;
     LowpK* dk = nullptr;         // device copies [2]
     DevBox* box16 = nullptr;     // the level's boxes in the padded layout
-    // step variants: 0 two-pass, 1.. fused with runs of FUSED_ZC[v - 1] planes
-    FusedTile* ftiles[3] = {nullptr, nullptr, nullptr};
-    int nftiles[3] = {0, 0, 0};
+    // step variants (FUSED_ZC): fused tile lists of variants 1 and 2
+    FusedTile* ftiles[2] = {nullptr, nullptr};
+    int nftiles[2] = {0, 0};
     int variant = 0;
     double variant_ms[4] = {0, 0, 0, 0};   // tuner's timings (0: not timed)
     float* qs = nullptr;         // Q_corr of the two-pass step, [3][N]
@@ -342,7 +342,7 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     D->nhalo = (long long)halo.size();
     mbg_status st;
     if ((st = lalloc(L, (void**)&D->box16, box.size() * sizeof(DevBox), err)) != MBG_OK) return st;
-    for (int v = 0; v < 3; ++v) {
+    for (int v = 0; v < 2; ++v) {
         const std::vector<FusedTile> tiles = fused_tiles(box, FUSED_ZC[v]);
         D->nftiles[v] = (int)tiles.size();
         if ((st = lalloc(L, (void**)&D->ftiles[v], tiles.size() * sizeof(FusedTile), err)) != MBG_OK) return st;
@@ -544,11 +544,13 @@ int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const Le
         });
         ++launches;
     }
-    if (D->variant == 0) {
+    if (D->variant == 0 || D->variant == 3) {
+        const int tight = D->variant == 3;
         run(LOWP_STAGE_FUSED,
             [&] {
                 const QPtrs qp = make_qptrs(L.f[A], L.g[A], L.f[1 - A], L.g[1 - A], L.N);
-                LOWP16(bf, two_pass, k, D->ct, D->lat, plan.tiles, plan.ntiles, D->halo, D->nhalo, D->qs, qp, s);
+                LOWP16(bf, two_pass, k, D->ct, D->lat, plan.tiles, plan.ntiles, D->halo, D->nhalo, D->qs, qp, tight,
+                       s);
             });
         launches += 3;
     } else {

@@ -53,8 +53,9 @@ using LowpRunner = std::function<void(int stage, const std::function<void()>& la
 int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const LevelPlan& plan, double dt,
                  const double idx[3], const CoalesceCell* coal, long long ncoal, const LowpLevel* fine,
                  const LevelPlan* fplan, cudaStream_t s, const LowpRunner& run);
-// step variants (0: two-pass, 1..3: fused with 4, 8, 16-plane runs) and the
-// tuner that times them on the level's data and keeps the fastest
+// step variants (0: two-pass, 1..2: fused with 4- or 8-plane runs, 3:
+// two-pass with a tighter register cap) and the tuner that times them on the
+// level's data and keeps the fastest
 int lowp_variants();
 mbg_status lowp_autotune(LowpLevel& L, const LevelPlan& plan, const BCParams& bc, const CoalesceCell* coal,
                          long long ncoal, const LowpLevel* fine, const LevelPlan* fplan, int reps, cudaStream_t s,

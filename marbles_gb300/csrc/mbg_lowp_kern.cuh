@@ -610,8 +610,8 @@ __global__ void k_qhalo16(const LowpK* __restrict__ K, const HaloCell* __restric
     qs[d * L.N + hc] = v;
 }
 
-template <bool BF>
-__global__ void __launch_bounds__(TILE_CELLS, 5)
+template <bool BF, int MINB>
+__global__ void __launch_bounds__(TILE_CELLS, MINB)
     k_collide16(const LowpK* __restrict__ K, const CodecTab ct, const Lattice<float> lat,
                 const Tile* __restrict__ tiles, const float* __restrict__ qs, const QPtrs qp)
 {
@@ -1003,12 +1003,15 @@ int Lowp16<BF>::fused_blocks_per_sm()
 }
 template <bool BF>
 void Lowp16<BF>::two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
-                          int ntiles, const HaloCell* h, long long nh, float* qs, const QPtrs& qp, cudaStream_t s)
+                          int ntiles, const HaloCell* h, long long nh, float* qs, const QPtrs& qp, int tight,
+                          cudaStream_t s)
 {
     if (ntiles == 0) return;
     k_qcorr16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, tiles, qs, qp);
     if (nh > 0) k_qhalo16<BF><<<(unsigned)((nh + 127) / 128), 128, 0, s>>>(k, h, nh, qs);
-    k_collide16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs, qp);
+    // register cap: 5 resident blocks per SM, or 6 with tight
+    if (tight) k_collide16<BF, 6><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs, qp);
+    else k_collide16<BF, 5><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs, qp);
 }
 template <bool BF>
 void Lowp16<BF>::ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s)

@@ -52,7 +52,9 @@ struct FusedTile {
 
 // host helpers of the layout (mbg_lowp.cu), shared with the batched domains
 // (mbg_batch.cu)
-constexpr int FUSED_ZC[3] = {4, 8, 16};   // plane runs of the fused step variants 1..3
+// step variants: 0 two-pass, 1 and 2 fused with runs of FUSED_ZC[v - 1]
+// planes, 3 two-pass with the collision pass capped at 80 registers
+constexpr int FUSED_ZC[2] = {4, 8};
 CodecTab make_codec(const mbg_params& p);
 Phys32 phys32(const mbg_params& p, double dt, const double idx[3]);
 long long pad_boxes(std::vector<DevBox>& box);
@@ -92,7 +94,8 @@ struct Lowp16 {
     static int fused_blocks_per_sm();   // resident CTAs of the fused step per SM
     // the two-pass step: Q_corr pass, pad of Q_corr, collision pass (3 launches)
     static void two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
-                         int ntiles, const HaloCell* h, long long nh, float* qs, const QPtrs& qp, cudaStream_t s);
+                         int ntiles, const HaloCell* h, long long nh, float* qs, const QPtrs& qp, int tight,
+                         cudaStream_t s);
     static void ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s);
     // the ghost stream through its plan: gather, then the general entries
     static void ghost_gather(const LowpK* k, const long long* dst, const long long* src, long long n,
