@@ -391,10 +391,15 @@ def roofline(res, form):
     if name == "k_moments":
         per_cell = 432 + 1 if form == "fp64" else per_cell
     achieved = per_cell * cells / (kv["ms"] * 1e-3) / 1e9
+    # DRAM bytes of one average launch of the class: the per-cell-update
+    # figure measured by ncu on the profiling case (profiles/traffic.json)
+    # times the cell-updates per launch here
     traffic = None
     tp = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tp):
-        traffic = json.load(open(tp)).get(form, {}).get(name)
+        t = json.load(open(tp)).get(form, {}).get(name)
+        if t and kv.get("launches"):
+            traffic = t["bytes_per_cell_update"] * cells / kv["launches"]
     return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if not pk.get("fallback") else "fallback",
