@@ -701,12 +701,14 @@ static mbg_status explode(mbg_ctx* ctx, int lev)
     Level& F = ctx->lv[lev];
     Level& C = ctx->lv[lev - 1];
     if (ctx->p.precision != MBG_FP64) {
-        timed(ctx, TK_EXPLODE, [&] { lowp_explode(F.lowp, F.plan, C.lowp, C.plan, ctx->s); });
+        int n = 0;
+        timed(ctx, TK_EXPLODE, [&] { n = lowp_explode(F.lowp, F.plan, C.lowp, C.plan, ctx->s); });
+        ctx->launches += n;
     } else {
         timed(ctx, TK_EXPLODE,
               [&] { launch_explode(F.plan, C.plan, C.f[C.cur], C.g[C.cur], F.fg[F.cur], F.gg[F.cur], ctx->s); });
+        ctx->launches++;
     }
-    ctx->launches++;
     MBG_CUDA(cudaGetLastError());
     return MBG_OK;
 }

@@ -36,14 +36,12 @@ __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, BCParams P, Phys64
     MomentAcc<double> acc;
 #define MBG_M64(q)                                                             \
     {                                                                          \
-        double fq, gq;                                                         \
-        if (ovr) {                                                             \
-            fq = fB[q * L.N + cell];                                           \
-            gq = gB[q * L.N + cell];                                           \
-        } else {                                                               \
+        double fq = ovr ? fB[q * L.N + cell] : 0.0;                            \
+        double gq = ovr ? gB[q * L.N + cell] : 0.0;                            \
+        if (!ovr || is_noovr(fq))                                              \
             fq = pull<q>(L, P, B, x, y, z, tf, interior, fA, fAg, false, ph.lat); \
+        if (!ovr || is_noovr(gq))                                              \
             gq = pull<q>(L, P, B, x, y, z, tf, interior, gA, gAg, true, ph.lat);  \
-        }                                                                      \
         acc.template add<q>(fq, gq);                                           \
     }
     MBG_UNROLL27(MBG_M64)
@@ -86,9 +84,10 @@ __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, BCParams P, Phys64
     const bool ovr = tf & FL_OVR;
     if (!(tf & FL_FLUID)) {
         // solid cells keep the stream's sentinel (or the coalesced value)
-        if (!ovr) {
 #pragma unroll
-            for (int q = 0; q < NQ; ++q) { fB[q * N + cell] = -1.0; gB[q * N + cell] = -1.0; }
+        for (int q = 0; q < NQ; ++q) {
+            if (!ovr || is_noovr(fB[q * N + cell])) fB[q * N + cell] = -1.0;
+            if (!ovr || is_noovr(gB[q * N + cell])) gB[q * N + cell] = -1.0;
         }
         return;
     }
@@ -117,13 +116,15 @@ __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, BCParams P, Phys64
         build_equilibrium<double>(m, dqx, dqy, dqz, ph.nu, ph.alpha, ph.dt, ph.Rg, ph.cv, ph.lat, E);
 #define MBG_RF64(q)                                                                                  \
     {                                                                                                \
-        const double fq = ovr ? fB[q * N + cell] : pull<q>(L, P, B, x, y, z, tf, interior, fA, fAg, false, ph.lat); \
+        double fq = ovr ? fB[q * N + cell] : 0.0;                                                    \
+        if (!ovr || is_noovr(fq)) fq = pull<q>(L, P, B, x, y, z, tf, interior, fA, fAg, false, ph.lat); \
         const double feq = E.template feq<q>();                                                      \
         fB[q * N + cell] = fq + omega * (feq - fq);                                                  \
     }
 #define MBG_RG64(q)                                                                                  \
     {                                                                                                \
-        const double gq = ovr ? gB[q * N + cell] : pull<q>(L, P, B, x, y, z, tf, interior, gA, gAg, true, ph.lat); \
+        double gq = ovr ? gB[q * N + cell] : 0.0;                                                    \
+        if (!ovr || is_noovr(gq)) gq = pull<q>(L, P, B, x, y, z, tf, interior, gA, gAg, true, ph.lat); \
         const double geq = E.template geq<q>(ph.lat);                                                \
         gB[q * N + cell] = gq + omega * (geq - gq);                                                  \
     }

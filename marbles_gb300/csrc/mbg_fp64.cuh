@@ -11,6 +11,12 @@ namespace mbg {
 
 using LV = LevelView<double>;
 
+// override value of a (coarse cell, direction) whose eight fine children were
+// all masked: the step pulls the cell's own streamed value there (a NaN bit
+// pattern that arithmetic does not produce)
+constexpr long long NOOVR64 = (long long)0xFFF8000000000FFDULL;
+__device__ __forceinline__ bool is_noovr(double v) { return __double_as_longlong(v) == NOOVR64; }
+
 // pulled (post-stream) value of direction q at box-local target (x,y,z)
 template <int q>
 __device__ __forceinline__ double pull(const LV& L, const BCParams& P, const DevBox& B, int x, int y, int z,

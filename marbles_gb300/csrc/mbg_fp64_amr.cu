@@ -76,26 +76,11 @@ __global__ void k_explode(LV F, LV C, const GhostCell* gl, long long n, const do
     }
 }
 
-// streamed value of a runtime direction (the coalescence's fallback where
-// every child is masked)
-__device__ __noinline__ double pull_rt(int q, const LV& C, const BCParams& P, const DevBox& O, int x, int y, int z,
-                                       uint8_t tf, const double* v, const double* vg, bool is_g,
-                                       const Lattice<double>& lat)
-{
-    switch (q) {
-#define MBG_PRT(qq) \
-    case qq: return pull<qq>(C, P, O, x, y, z, tf, false, v, vg, is_g, lat);
-        MBG_UNROLL27(MBG_PRT)
-#undef MBG_PRT
-    }
-    return -1.0;
-}
-
 // ---- coalescence: masked average of the 8 fine children --------------------
 // (masked_avgdown, Source/Utilities.H:315-350).  into_state: write into the
 // coarse state buffer directly (initial average_down, ng = 0); otherwise into
-// the coarse post-stream override buffer, with the coarse streamed value
-// where every child is masked.  One thread per (coarse cell, direction):
+// the coarse post-stream override buffer, with the code NOOVR64 where every
+// child is masked (the step then pulls the coarse cell's own streamed value).  One thread per (coarse cell, direction):
 // blockIdx.y is the direction, so a warp reads one component of 32
 // consecutive coarse cells' children.
 __global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, const CoalesceCell* cl, long long n,
@@ -138,8 +123,7 @@ __global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, const CoalesceCell
         double r;
         if (vol > 0.0) r = s / vol;
         else if (into_state) r = cA[q * C.N + cell];
-        else r = pull_rt(q, C, P, O, cc.cx, cc.cy, cc.cz, flag_at(C, O, cc.cx, cc.cy, cc.cz), cA,
-                         lat ? gcAg : fcAg, lat == 1, ph.lat);
+        else r = __longlong_as_double(NOOVR64);   // the step pulls the cell's own streamed value
         (lat ? gcB : fcB)[q * C.N + cell] = r;
     }
 }

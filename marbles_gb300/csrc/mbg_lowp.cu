@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <unordered_map>
 
 #include "mbg_lowp_types.cuh"
 
@@ -45,6 +46,7 @@ struct LowpDev {
     long long nhalo = 0;
     u16* fo = nullptr;           // coalescence override buffers
     u16* go = nullptr;
+    ExplodePlan xp{};            // explosion into this (fine) level's ghost fabs
 };
 
 static LowpDev* dev_of(LowpLevel& L) { return (LowpDev*)L.impl; }
@@ -313,6 +315,51 @@ static void ghost_plan(const std::vector<DevBox>& box, const std::vector<GhostCe
     }
 }
 
+// explosion plan: the distinct coarse cells under the uncovered ghost cells,
+// numbered in order of first use so that neighbouring ghost cells read
+// neighbouring slots
+static void explode_plan(const std::vector<DevBox>& box, const std::vector<GhostCell>& ghosts, const LevelHost& h,
+                         std::vector<XSlot>& xc, std::vector<int>& slot)
+{
+    auto floor2 = [](int v) { return v >= 0 ? v / 2 : -((1 - v) / 2); };
+    std::unordered_map<long long, int> id;
+    slot.reserve(ghosts.size());
+    for (const GhostCell& g : ghosts) {
+        const DevBox& B = box[g.box];
+        int fp[3] = {B.lo[0] + g.x, B.lo[1] + g.y, B.lo[2] + g.z};
+        // the device's wrap_pos: periodic sides wrap, up to the first side
+        // that is outside and not periodic
+        for (int d = 0; d < 3; ++d) {
+            if (fp[d] >= h.dlo[d] && fp[d] <= h.dhi[d]) continue;
+            if (!h.per[d]) break;
+            const int len = h.dhi[d] - h.dlo[d] + 1;
+            fp[d] = h.dlo[d] + (((fp[d] - h.dlo[d]) % len) + len) % len;
+        }
+        const XSlot c{floor2(fp[0]), floor2(fp[1]), floor2(fp[2]), 0};
+        const long long key = ((long long)(c.z + 32768) * 65536 + (c.y + 32768)) * 65536 + (c.x + 32768);
+        auto it = id.find(key);
+        if (it == id.end()) {
+            it = id.emplace(key, (int)xc.size()).first;
+            xc.push_back(c);
+        }
+        slot.push_back(it->second);
+    }
+}
+
+// order a gather plan by destination: component-major destinations make
+// consecutive entries write consecutive cells of one component (the plans are
+// built cell by cell, which spreads a warp's 2-byte stores over 27 components)
+static void sort_plan(std::vector<long long>& dst, std::vector<long long>& src)
+{
+    std::vector<std::pair<long long, long long>> e(dst.size());
+    for (size_t i = 0; i < dst.size(); ++i) e[i] = {dst[i], src[i]};
+    std::sort(e.begin(), e.end());
+    for (size_t i = 0; i < e.size(); ++i) {
+        dst[i] = e[i].first;
+        src[i] = e[i].second;
+    }
+}
+
 mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::vector<DevBox>& hbox, long long N,
                        long long NG, double dt, const double idx[3], const LevelHost& host, LowpLevel& L,
                        std::string& err)
@@ -336,9 +383,11 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     std::vector<long long> gdst, gsrc;
     std::vector<HaloCell> general;
     halo_plan(box, halo, L.N, NG, host, gdst, gsrc, general);
+    sort_plan(gdst, gsrc);
     std::vector<long long> sdst, ssrc;
     std::vector<int> scell, sq;
     if (host.ghosts && NG > 0) ghost_plan(box, *host.ghosts, L.N, NG, host, sdst, ssrc, scell, sq);
+    sort_plan(sdst, ssrc);
     D->nhalo = (long long)halo.size();
     mbg_status st;
     if ((st = lalloc(L, (void**)&D->box16, box.size() * sizeof(DevBox), err)) != MBG_OK) return st;
@@ -367,6 +416,21 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     cudaMemcpy(D->ssrc, ssrc.data(), ssrc.size() * sizeof(long long), cudaMemcpyHostToDevice);
     cudaMemcpy(D->scell, scell.data(), scell.size() * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(D->sq, sq.data(), sq.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (host.ghosts && NG > 0 && !host.ghosts->empty()) {
+        std::vector<XSlot> xc;
+        std::vector<int> slot;
+        explode_plan(box, *host.ghosts, host, xc, slot);
+        ExplodePlan& xp = D->xp;
+        xp.n = (long long)slot.size();
+        xp.nx = (long long)xc.size();
+        if ((st = lalloc(L, (void**)&xp.slot, slot.size() * sizeof(int), err)) != MBG_OK) return st;
+        if ((st = lalloc(L, (void**)&xp.xc, xc.size() * sizeof(XSlot), err)) != MBG_OK) return st;
+        if ((st = lalloc(L, (void**)&xp.ix, (size_t)xp.nx * 7 * sizeof(int), err)) != MBG_OK) return st;
+        if ((st = lalloc(L, (void**)&xp.xs, (size_t)xp.nx * 8 * NQ * sizeof(float), err)) != MBG_OK) return st;
+        if ((st = lalloc(L, (void**)&xp.al, (size_t)xp.nx * 6 * sizeof(float), err)) != MBG_OK) return st;
+        cudaMemcpy((void*)xp.slot, slot.data(), slot.size() * sizeof(int), cudaMemcpyHostToDevice);
+        cudaMemcpy((void*)xp.xc, xc.data(), xc.size() * sizeof(XSlot), cudaMemcpyHostToDevice);
+    }
     cudaMemcpy(D->box16, box.data(), box.size() * sizeof(DevBox), cudaMemcpyHostToDevice);
     cudaMemcpy(D->halo, halo.data(), halo.size() * sizeof(HaloCell), cudaMemcpyHostToDevice);
     const size_t sb = (size_t)L.N * NQ * 2;
@@ -623,9 +687,9 @@ void lowp_variant(LowpLevel& L, int* variant, double ms[4])
     for (int v = 0; v < 4; ++v) ms[v] = D->variant_ms[v];
 }
 
-void lowp_explode(LowpLevel& F, const LevelPlan& fplan, const LowpLevel& C, const LevelPlan& cplan, cudaStream_t s)
+int lowp_explode(LowpLevel& F, const LevelPlan& fplan, const LowpLevel& C, const LevelPlan& cplan, cudaStream_t s)
 {
-    if (fplan.nghost_cells == 0) return;
+    if (fplan.nghost_cells == 0 || dev_of(F)->xp.nx == 0) return 0;
     LowpLevel& Cm = const_cast<LowpLevel&>(C);
     LowpDev* FD = dev_of(F);
     LowpDev* CD = dev_of(Cm);
@@ -633,8 +697,10 @@ void lowp_explode(LowpLevel& F, const LevelPlan& fplan, const LowpLevel& C, cons
     ensure_k(Cm, cplan, known_bc(Cm), CD->with_override, s);
     const LowpK* kf = FD->dk + F.cur;
     const LowpK* kc = CD->dk + C.cur;
-    LOWP16(F.precision == MBG_FP32C_BF16S, explode, kf, kc, fplan.ghost_list, fplan.nghost_cells, (u16*)F.fg[F.cur],
-           (u16*)F.gg[F.cur], s);
+    ExplodePlan xp = FD->xp;
+    xp.gl = fplan.ghost_list;
+    LOWP16(F.precision == MBG_FP32C_BF16S, explode, kf, kc, xp, (u16*)F.fg[F.cur], (u16*)F.gg[F.cur], s);
+    return 3;
 }
 
 void lowp_average_down(LowpLevel& C, const LevelPlan& cplan, const LowpLevel& F, const LevelPlan& fplan,

@@ -61,7 +61,8 @@ mbg_status lowp_autotune(LowpLevel& L, const LevelPlan& plan, const BCParams& bc
                          long long ncoal, const LowpLevel* fine, const LevelPlan* fplan, int reps, cudaStream_t s,
                          std::string& err);
 void lowp_variant(LowpLevel& L, int* variant, double ms[4]);
-void lowp_explode(LowpLevel& F, const LevelPlan& fplan, const LowpLevel& C, const LevelPlan& cplan, cudaStream_t s);
+// returns the number of kernels launched
+int lowp_explode(LowpLevel& F, const LevelPlan& fplan, const LowpLevel& C, const LevelPlan& cplan, cudaStream_t s);
 void lowp_average_down(LowpLevel& C, const LevelPlan& cplan, const LowpLevel& F, const LevelPlan& fplan,
                        const CoalesceCell* list, long long n, cudaStream_t s);
 

@@ -63,7 +63,7 @@ __device__ __forceinline__ u16 enc(const CodecTab& ct, float v, int q, bool g)
     if (v == -1.0f) return SENT16;
     const float h = g ? (v - ct.grest[q]) * ct.gisc[q] : (v - ct.frest[q]) * ct.fisc[q];
     const u16 r = f2h<BF>(h);
-    return r == SENT16 ? (u16)0xFFFEu : r;
+    return (r == SENT16 || r == NOOVR16) ? (u16)0xFFFEu : r;
 }
 
 
@@ -106,14 +106,12 @@ __device__ __noinline__ MomentAcc<float> moments16_slow(const LowpK* __restrict_
     const long long cell = B.voff + (in_valid<u16>(B, x, y, z) ? val_lin(B, x, y, z) : 0);
 #define MBG_MS16(q)                                                                  \
     {                                                                                \
-        float fq, gq;                                                                \
-        if (ovr) {                                                                   \
-            fq = dec<BF>(K->ct, K->s.fo[q * L.N + cell], q, false);                  \
-            gq = dec<BF>(K->ct, K->s.go[q * L.N + cell], q, true);                   \
-        } else {                                                                     \
-            fq = pull16_slow<q, BF>(K, b, x, y, z, tf, 0);                           \
-            gq = pull16_slow<q, BF>(K, b, x, y, z, tf, 1);                           \
-        }                                                                            \
+        const u16 of = ovr ? K->s.fo[q * L.N + cell] : NOOVR16;                       \
+        const u16 og = ovr ? K->s.go[q * L.N + cell] : NOOVR16;                       \
+        const float fq = of != NOOVR16 ? dec<BF>(K->ct, of, q, false)                 \
+                                       : pull16_slow<q, BF>(K, b, x, y, z, tf, 0);    \
+        const float gq = og != NOOVR16 ? dec<BF>(K->ct, og, q, true)                  \
+                                       : pull16_slow<q, BF>(K, b, x, y, z, tf, 1);    \
         acc.template add<q>(fq, gq);                                                 \
     }
     MBG_UNROLL27(MBG_MS16)
@@ -248,14 +246,20 @@ __device__ __noinline__ MomentAcc<float> moments_cell(const LowpK* __restrict__ 
     const long long c = B.voff + val_lin(B, x, y, z);
     const CodecTab& ct = K->ct;
     MomentAcc<float> acc;
+    const bool vf = B.vfluid;
     if ((tf & FL_OVR) && K->s.fo) {
-#define MBG_MO16(q) \
-    acc.template add<q>(dec<BF>(ct, K->s.fo[q * L.N + c], q, false), dec<BF>(ct, K->s.go[q * L.N + c], q, true));
+#define MBG_MO16(q)                                                                                 \
+    {                                                                                               \
+        const u16 of = K->s.fo[q * L.N + c], og = K->s.go[q * L.N + c];                             \
+        acc.template add<q>(of != NOOVR16 ? dec<BF>(ct, of, q, false)                               \
+                                          : pullp<q, BF>(ct, L, B, K->s.f, c, x, y, z, vf, false),  \
+                            og != NOOVR16 ? dec<BF>(ct, og, q, true)                                \
+                                          : pullp<q, BF>(ct, L, B, K->s.g, c, x, y, z, vf, true));  \
+    }
         MBG_UNROLL27(MBG_MO16)
 #undef MBG_MO16
         return acc;
     }
-    const bool vf = B.vfluid;
 #define MBG_MC16(q)                                                                     \
     acc.template add<q>(pullp<q, BF>(ct, L, B, K->s.f, c, x, y, z, vf, false),          \
                         pullp<q, BF>(ct, L, B, K->s.g, c, x, y, z, vf, true));
@@ -306,7 +310,10 @@ __device__ __noinline__ float pull_gen(const LowpK* __restrict__ K, int b, int x
     const long long c = B.voff + val_lin(B, x, y, z);
     const bool is_g = which & 1;
     const uint8_t tf = flag_at(L, B, x, y, z);
-    if ((tf & FL_OVR) && K->s.fo) return dec<BF>(K->ct, (is_g ? K->s.go : K->s.fo)[q * L.N + c], q, is_g);
+    if ((tf & FL_OVR) && K->s.fo) {
+        const u16 o = (is_g ? K->s.go : K->s.fo)[q * L.N + c];
+        if (o != NOOVR16) return dec<BF>(K->ct, o, q, is_g);
+    }
     return pullp<q, BF>(K->ct, L, B, is_g ? K->s.g : K->s.f, c, x, y, z, B.vfluid, is_g);
 }
 
@@ -439,8 +446,10 @@ __global__ void __launch_bounds__(FT_THREADS, 2)
                 if (!(prevf & FL_FLUID)) {
 #define MBG_SOL16(q)                                                \
     {                                                               \
-        fB[q * N + c] = ovr ? sfo[q * N + c] : SENT16;              \
-        gB[q * N + c] = ovr ? sgo[q * N + c] : SENT16;              \
+        const u16 of = ovr ? sfo[q * N + c] : SENT16;               \
+        const u16 og = ovr ? sgo[q * N + c] : SENT16;               \
+        fB[q * N + c] = of == NOOVR16 ? SENT16 : of;                \
+        gB[q * N + c] = og == NOOVR16 ? SENT16 : og;                \
     }
                     MBG_UNROLL27(MBG_SOL16)
 #undef MBG_SOL16
@@ -631,8 +640,10 @@ __global__ void __launch_bounds__(TILE_CELLS, MINB)
     if (!(tf & FL_FLUID)) {
 #define MBG_SOLC16(q)                                               \
     {                                                               \
-        fB[q * N + c] = ovr ? sfo[q * N + c] : SENT16;              \
-        gB[q * N + c] = ovr ? sgo[q * N + c] : SENT16;              \
+        const u16 of = ovr ? sfo[q * N + c] : SENT16;               \
+        const u16 og = ovr ? sgo[q * N + c] : SENT16;               \
+        fB[q * N + c] = of == NOOVR16 ? SENT16 : of;                \
+        gB[q * N + c] = og == NOOVR16 ? SENT16 : og;                \
     }
         MBG_UNROLL27(MBG_SOLC16)
 #undef MBG_SOLC16
@@ -757,16 +768,75 @@ __device__ __forceinline__ long long crse16_index(const LV16& C, const int p0[3]
     return O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2]);
 }
 
+// Explosion (cell_cons_interp restated: one MC-limited slope per axis, the
+// limiter shared by the 27 components of a lattice) in three launches.  The
+// slopes and the limiter depend only on the coarse cell, so they are computed
+// once per coarse cell under the ghost shell rather than once per fine child;
+// each child then evaluates the same expression.
+//
+// 1. the 7 coarse storage indices (centre, -x, +x, -y, +y, -z, +z) of each
+//    slot, -1 where the coarse level has no cell; limiter reset to 1
 template <bool BF>
-__global__ void k_explode16(const LowpK* __restrict__ KF, const LowpK* __restrict__ KC, const GhostCell* gl,
-                            long long n, u16* fg, u16* gg)
+__global__ void k_xindex16(const LowpK* __restrict__ KC, const XSlot* __restrict__ xc, long long nx,
+                           int* __restrict__ ix, float* __restrict__ al)
 {
-    // one thread per fine ghost cell: neighbouring threads read neighbouring
-    // coarse cells, so every component's loads coalesce
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nx) return;
+    const LV16& C = KC->L;
+    const XSlot c = xc[e];
+    const int cp[3] = {c.x, c.y, c.z};
+    ix[e] = (int)crse16_index<BF>(C, cp, 0, 0);
+    for (int d = 0; d < 3; ++d) {
+        ix[(1 + 2 * d) * nx + e] = (int)crse16_index<BF>(C, cp, d, -1);
+        ix[(2 + 2 * d) * nx + e] = (int)crse16_index<BF>(C, cp, d, 1);
+    }
+    for (int k = 0; k < 6; ++k) al[k * nx + e] = 1.0f;
+}
+
+// 2. per (slot, direction): value, centred slopes, and each axis' limiter
+//    ratio folded into the slot's minimum (non-negative floats order like
+//    their bit patterns, so an integer atomicMin is exact and order-free)
+template <bool BF>
+__global__ void k_xslope16(const LowpK* __restrict__ KC, const int* __restrict__ ix, long long nx,
+                           float* __restrict__ xs, float* __restrict__ al)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    if (e >= nx) return;
+    const LV16& C = KC->L;
+    int id[7];
+    for (int k = 0; k < 7; ++k) id[k] = ix[k * nx + e];
+    for (int lat = 0; lat < 2; ++lat) {
+        const bool isg = lat == 1;
+        const u16* __restrict__ v = (isg ? KC->s.g : KC->s.f) + (long long)q * C.N;
+        float u[7];
+        for (int k = 0; k < 7; ++k) u[k] = id[k] >= 0 ? dec<BF>(KC->ct, v[id[k]], q, isg) : 0.0f;
+        float* o = xs + ((long long)(lat * 4) * NQ + q) * nx + e;
+        o[0] = u[0];
+        for (int d = 0; d < 3; ++d) {
+            const float u0 = u[0], um = u[1 + 2 * d], up = u[2 + 2 * d];
+            const float cen = 0.5f * (up - um);
+            const float forw = 2.0f * (up - u0);
+            const float back = 2.0f * (u0 - um);
+            const float slp = (forw * back >= 0.f) ? fminf(fabsf(forw), fabsf(back)) : 0.f;
+            o[(long long)(1 + d) * NQ * nx] = cen;
+            if (cen != 0.f) {
+                const float r = fminf(slp, fabsf(cen)) / fabsf(cen);
+                if (r < 1.0f) atomicMin((int*)&al[(lat * 3 + d) * nx + e], __float_as_int(r));
+            }
+        }
+    }
+}
+
+// 3. one thread per fine ghost cell: u0 + sum_d off_d (alpha_d slope_d)
+template <bool BF>
+__global__ void k_xfill16(const LowpK* __restrict__ KF, const GhostCell* __restrict__ gl,
+                          const int* __restrict__ slot, long long n, const float* __restrict__ xs,
+                          const float* __restrict__ al, long long nx, u16* __restrict__ fg, u16* __restrict__ gg)
+{
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
     const LV16& F = KF->L;
-    const LV16& C = KC->L;
     const GhostCell g = gl[e];
     const DevBox& B = F.box[g.box];
     int fp[3] = {B.lo[0] + g.x, B.lo[1] + g.y, B.lo[2] + g.z};
@@ -775,43 +845,26 @@ __global__ void k_explode16(const LowpK* __restrict__ KF, const LowpK* __restric
     const float off[3] = {((fp[0] - 2 * cp[0]) + 0.5f) / 2.0f - 0.5f, ((fp[1] - 2 * cp[1]) + 0.5f) / 2.0f - 0.5f,
                           ((fp[2] - 2 * cp[2]) + 0.5f) / 2.0f - 0.5f};
     const long long gi = B.goff + fab_lin(B, g.x, g.y, g.z);
-    long long ix[7];
-    ix[0] = crse16_index<BF>(C, cp, 0, 0);
-    for (int d = 0; d < 3; ++d) {
-        ix[1 + 2 * d] = crse16_index<BF>(C, cp, d, -1);
-        ix[2 + 2 * d] = crse16_index<BF>(C, cp, d, 1);
-    }
+    const long long sl = slot[e];
     for (int lat = 0; lat < 2; ++lat) {
         const bool isg = lat == 1;
-        const u16* v = isg ? KC->s.g : KC->s.f;
-        u16* out = isg ? gg : fg;
-        auto at = [&](int k, int q) { return ix[k] >= 0 ? dec<BF>(KC->ct, v[q * C.N + ix[k]], q, isg) : 0.0f; };
-        float alpha[3] = {1.f, 1.f, 1.f};
+        u16* __restrict__ out = isg ? gg : fg;
+        const float a0 = al[(lat * 3 + 0) * nx + sl], a1 = al[(lat * 3 + 1) * nx + sl],
+                    a2 = al[(lat * 3 + 2) * nx + sl];
+        const float* __restrict__ x = xs + (long long)(lat * 4) * NQ * nx + sl;
+#pragma unroll 3
         for (int q = 0; q < NQ; ++q) {
-            float u[7];
-            for (int k = 0; k < 7; ++k) u[k] = at(k, q);
-            for (int d = 0; d < 3; ++d) {
-                const float u0 = u[0], um = u[1 + 2 * d], up = u[2 + 2 * d];
-                const float cen = 0.5f * (up - um);
-                const float forw = 2.0f * (up - u0);
-                const float back = 2.0f * (u0 - um);
-                const float slp = (forw * back >= 0.f) ? fminf(fabsf(forw), fabsf(back)) : 0.f;
-                if (cen != 0.f) alpha[d] = fminf(alpha[d], fminf(slp, fabsf(cen)) / fabsf(cen));
-            }
-        }
-        for (int q = 0; q < NQ; ++q) {
-            const float u0 = at(0, q);
-            const float cx = 0.5f * (at(2, q) - at(1, q));
-            const float cy = 0.5f * (at(4, q) - at(3, q));
-            const float cz = 0.5f * (at(6, q) - at(5, q));
-            out[q * F.NG + gi] =
-                enc<BF>(KF->ct, u0 + off[0] * (alpha[0] * cx) + off[1] * (alpha[1] * cy) + off[2] * (alpha[2] * cz),
-                        q, isg);
+            const float u0 = x[(long long)q * nx];
+            const float cx = x[(long long)(NQ + q) * nx];
+            const float cy = x[(long long)(2 * NQ + q) * nx];
+            const float cz = x[(long long)(3 * NQ + q) * nx];
+            out[q * F.NG + gi] = enc<BF>(KF->ct, u0 + off[0] * (a0 * cx) + off[1] * (a1 * cy) + off[2] * (a2 * cz),
+                                         q, isg);
         }
     }
 }
 
-// streamed value of a runtime direction (the coalescence's fallback)
+// streamed value of a runtime direction (the ghost stream's general entries)
 template <bool BF>
 __device__ __noinline__ float pull16_rt(int q, const LowpK* __restrict__ K, int b, int x, int y, int z,
                                         uint8_t tflag, int which)
@@ -828,9 +881,26 @@ __device__ __noinline__ float pull16_rt(int q, const LowpK* __restrict__ K, int 
 // coalescence: FP64 masked average of the 8 fine children into the override
 // buffer (advance) or the coarse state (initial average_down); one thread per
 // (coarse cell, direction), blockIdx.y the direction
+// exact FP32 -> FP64 widening with integer operations (IEEE-754 binary32 to
+// binary64: rebias the exponent by 1023 - 127 = 896, widen the fraction);
+// zero, subnormal and non-finite inputs take the hardware conversion.  The
+// FP64 pipe of GB300 issues 2 operations per SM per clock, so the
+// coalescence keeps it for the sums alone.
+__device__ __forceinline__ double widen_exact(float v)
+{
+    const unsigned u = __float_as_uint(v);
+    const unsigned ex = (u >> 23) & 0xFFu;
+    if (ex == 0u || ex == 0xFFu) return (double)v;
+    const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
+                                    ((unsigned long long)(ex + 896u) << 52) |
+                                    ((unsigned long long)(u & 0x7FFFFFu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
 template <bool BF>
-__global__ void k_coalesce16(const LowpK* __restrict__ KC, const LowpK* __restrict__ KF, const CoalesceCell* cl,
-                             long long n, u16* fo, u16* go, int into_state)
+__global__ void __launch_bounds__(128) k_coalesce16(const LowpK* __restrict__ KC, const LowpK* __restrict__ KF,
+                                                    const CoalesceCell* __restrict__ cl, long long n,
+                                                    u16* __restrict__ fo, u16* __restrict__ go, int into_state)
 {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
@@ -841,28 +911,48 @@ __global__ void k_coalesce16(const LowpK* __restrict__ KC, const LowpK* __restri
     const DevBox& O = C.box[cc.cbox];
     const DevBox& A = F.box[cc.fbox];
     const long long cell = O.voff + val_lin(O, cc.cx, cc.cy, cc.cz);
-    // the mask test |v - (-1)| > SMALL_NUM on the FP32 decoded value; the sum in FP64
+    // the eight children's codes of both lattices, child k = 4 kz + 2 ky + kx;
+    // fixed offsets when all eight are valid cells of box A (the common case)
+    u16 code[2][8];
+    if (cc.fx >= 0 && cc.fy >= 0 && cc.fz >= 0 && cc.fx + 1 < A.n[0] && cc.fy + 1 < A.n[1] && cc.fz + 1 < A.n[2]) {
+        const long long b = (long long)q * F.N + A.voff + val_lin(A, cc.fx, cc.fy, cc.fz);
+        const int sy = A.sy, sz = A.sz;
+        const u16* __restrict__ f = KF->s.f + b;
+        const u16* __restrict__ g = KF->s.g + b;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int off = (k >> 2) * sz + ((k >> 1) & 1) * sy + (k & 1);
+            code[0][k] = __ldg(f + off);
+            code[1][k] = __ldg(g + off);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int x = cc.fx + (k & 1), y = cc.fy + ((k >> 1) & 1), z = cc.fz + (k >> 2);
+            code[0][k] = fab_value(F, A, x, y, z, q, KF->s.f, KF->s.fg);
+            code[1][k] = fab_value(F, A, x, y, z, q, KF->s.g, KF->s.gg);
+        }
+    }
+    // the mask test |v - (-1)| > SMALL_NUM on the FP32 decoded value; the sum
+    // in FP64, children in the reference's loop order (z, y, x)
     const float small_num = (float)(2.220446049250313e-16 * 1e10);
+#pragma unroll
     for (int lat = 0; lat < 2; ++lat) {
         const bool isg = lat == 1;
-        const u16* v = isg ? KF->s.g : KF->s.f;
-        const u16* vg = isg ? KF->s.gg : KF->s.fg;
         double sum = 0.0;
         int vol = 0;
-        for (int kr = 0; kr < 2; ++kr)
-            for (int jr = 0; jr < 2; ++jr)
-                for (int ir = 0; ir < 2; ++ir) {
-                    const float fv =
-                        dec<BF>(KF->ct, fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg), q, isg);
-                    if (fabsf(fv + 1.0f) > small_num) { sum += (double)fv; ++vol; }
-                }
-        // all eight children unmasked is the common case: sum / 8 is the
-        // exact product sum * 0.125, no FP64 division
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float fv = dec<BF>(KF->ct, code[lat][k], q, isg);
+            if (fabsf(fv + 1.0f) > small_num) { sum += widen_exact(fv); ++vol; }
+        }
+        // all eight children unmasked is the common case: sum / 8 is exact,
+        // and a power-of-two scaling commutes with the rounding to FP32 (the
+        // values are far from the FP32 range limits), so it is applied after
         u16 r;
-        if (vol > 0) r = enc<BF>(KC->ct, (float)(vol == 8 ? sum * 0.125 : sum / (double)vol), q, isg);
+        if (vol > 0) r = enc<BF>(KC->ct, vol == 8 ? __double2float_rn(sum) * 0.125f : (float)(sum / (double)vol), q, isg);
         else if (into_state) r = (isg ? KC->s.g : KC->s.f)[q * C.N + cell];
-        else r = enc<BF>(KC->ct, pull16_rt<BF>(q, KC, cc.cbox, cc.cx, cc.cy, cc.cz, flag_at(C, O, cc.cx, cc.cy, cc.cz),
-                                               isg ? 1 : 0), q, isg);
+        else r = NOOVR16;   // the step takes the cell's own streamed value
         (isg ? go : fo)[q * C.N + cell] = r;
     }
 }
@@ -1026,10 +1116,14 @@ void Lowp16<BF>::ghost_gather(const LowpK* k, const long long* dst, const long l
     if (ngen > 0) k_ghost_general16<BF><<<(unsigned)((ngen + 127) / 128), 128, 0, s>>>(k, gl, gcell, gq, ngen);
 }
 template <bool BF>
-void Lowp16<BF>::explode(const LowpK* kf, const LowpK* kc, const GhostCell* gl, long long n, u16* fg, u16* gg,
-                         cudaStream_t s)
+void Lowp16<BF>::explode(const LowpK* kf, const LowpK* kc, const ExplodePlan& xp, u16* fg, u16* gg, cudaStream_t s)
 {
-    if (n > 0) k_explode16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(kf, kc, gl, n, fg, gg);
+    if (xp.n <= 0 || xp.nx <= 0) return;
+    const unsigned bx = (unsigned)((xp.nx + 127) / 128);
+    k_xindex16<BF><<<bx, 128, 0, s>>>(kc, xp.xc, xp.nx, xp.ix, xp.al);
+    k_xslope16<BF><<<dim3(bx, NQ), 128, 0, s>>>(kc, xp.ix, xp.nx, xp.xs, xp.al);
+    k_xfill16<BF><<<(unsigned)((xp.n + 127) / 128), 128, 0, s>>>(kf, xp.gl, xp.slot, xp.n, xp.xs, xp.al, xp.nx, fg,
+                                                                  gg);
 }
 template <bool BF>
 void Lowp16<BF>::coalesce(const LowpK* kc, const LowpK* kf, const CoalesceCell* cl, long long n, u16* fo, u16* go,

@@ -11,6 +11,10 @@ using u16 = uint16_t;
 using LV16 = LevelView<u16>;
 
 constexpr u16 SENT16 = 0xFFFFu;
+// override code of a (coarse cell, direction) whose eight fine children were
+// all masked: the step takes the cell's own streamed value (a NaN pattern the
+// encoder never produces)
+constexpr u16 NOOVR16 = 0xFFFDu;
 constexpr int FT_THREADS = 256;   // threads of a fused-step CTA
 constexpr int FT_QX = 320;        // shared Q_corr rows: max over tw of th * (tw + 2)
 constexpr int FT_QY = 320;        // max over tw of (th + 2) * tw
@@ -41,6 +45,24 @@ struct LowpK {
 struct HaloCell {
     int box;
     short x, y, z, pad;
+};
+
+// explosion plan of a fine level: the distinct coarse cells under its
+// uncovered ghost cells (global coarse coordinates), each ghost cell's slot
+// among them, and per-slot scratch: the 7 coarse neighbours' storage indices
+// [7][nx], value and centred slopes [lattice][4][NQ][nx], limiter [lattice][3][nx]
+struct XSlot {
+    int x, y, z, pad;
+};
+struct ExplodePlan {
+    const GhostCell* gl;
+    const int* slot;
+    long long n;
+    const XSlot* xc;
+    int* ix;
+    float* xs;
+    float* al;
+    long long nx;
 };
 
 struct FusedTile {
@@ -100,8 +122,9 @@ struct Lowp16 {
     // the ghost stream through its plan: gather, then the general entries
     static void ghost_gather(const LowpK* k, const long long* dst, const long long* src, long long n,
                              const GhostCell* gl, const int* gcell, const int* gq, long long ngen, cudaStream_t s);
-    static void explode(const LowpK* kf, const LowpK* kc, const GhostCell* gl, long long n, u16* fg, u16* gg,
-                        cudaStream_t s);
+    // explosion: coarse neighbours, slopes and limiter per coarse cell, then
+    // the fine ghost cells (3 launches)
+    static void explode(const LowpK* kf, const LowpK* kc, const ExplodePlan& xp, u16* fg, u16* gg, cudaStream_t s);
     static void coalesce(const LowpK* kc, const LowpK* kf, const CoalesceCell* cl, long long n, u16* fo, u16* go,
                          int into_state, cudaStream_t s);
     static void encode(const LowpK* k, const Tile* tiles, int ntiles, const double* src, long long NV, u16* dst,
