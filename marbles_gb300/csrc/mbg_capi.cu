@@ -525,7 +525,14 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
                 const int cx = (int)(key % 65536), cy = (int)((key / 65536) % 65536), cz = (int)(key / 65536 / 65536);
                 int c[3] = {cx, cy, cz};
                 const int o = owner_host(C, c);
-                const int n = win[key];
+                // children that are valid cells of a fine box give the same
+                // values whichever box is named (reads go to their owner), so
+                // name that box: the kernels then read them at fixed offsets.
+                // Fine boxes are aligned to the ratio, so one box holds all
+                // eight.  The last-wins box stays for children in no box.
+                const int child[3] = {2 * cx, 2 * cy, 2 * cz};
+                const int own = owner_host(L, child);
+                const int n = own >= 0 ? own : win[key];
                 CoalesceCell cc;
                 cc.cbox = o;
                 cc.fbox = n;
