@@ -548,6 +548,14 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
                 const long long fi = CB.foff + ((long long)(cc.cz + 3) * (CB.n[1] + 6) + (cc.cy + 3)) * (CB.n[0] + 6) + (cc.cx + 3);
                 C.hflags[fi] |= (uint8_t)(ng == 1 ? (uint8_t)FL_OVR : (uint8_t)FL_COV);
             }
+            // cells whose children all lie in the named box first: each cell
+            // appears once, so the order changes no result, and warps then
+            // take the kernels' fixed-offset path together
+            std::stable_partition(cl.begin(), cl.end(), [&](const CoalesceCell& cc) {
+                const DevBox& A = L.hbox[cc.fbox];
+                return cc.fx >= 0 && cc.fy >= 0 && cc.fz >= 0 && cc.fx + 1 < A.n[0] && cc.fy + 1 < A.n[1] &&
+                       cc.fz + 1 < A.n[2];
+            });
             CoalesceCell** dst = ng ? &C.d_coal1 : &C.d_coal0;
             long long* cnt = ng ? &C.ncoal1 : &C.ncoal0;
             mbg_status st = dalloc(ctx, dst, cl.size());
