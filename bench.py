@@ -182,20 +182,30 @@ def run_form(form, steps, warmup, device_index):
            "kernels": {k: {"launches": n, "ms": t} for k, (n, t) in timing.items() if n},
            "clocks": clk.summary(), "tuning": tuning}
     # end to end through the C ABI with pinned host buffers: upload of the
-    # initial state, K steps each followed by the EB-force read-back (the
-    # reference computes it every step), download of the state
-    forces = torch.zeros(3, dtype=torch.float64, pin_memory=True)
+    # initial state, K steps each followed by a read-back of its result (FP64:
+    # the EB force, which the reference computes every step; 16-bit: the FP64
+    # conservation totals), download of the state.  One untimed round first:
+    # the first copies from freshly pinned buffers pay a one-time mapping cost
+    # (about 0.1 s on the GB300 machine), as the first steps pay for warm-up.
+    res_buf = torch.zeros(5, dtype=torch.float64, pin_memory=True)
+    rb = C.cast(res_buf.data_ptr(), dp)
+
+    def result():
+        fn = lib.mbg_eb_forces if form == "fp64" else lib.mbg_conserved
+        ctx._check(fn(ctx.h, rb), "result")
+
+    for lev, (f, g) in enumerate(host):
+        ctx._check(lib.mbg_set_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
+        ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+    result()
     ctx.synchronize()
     t0 = time.perf_counter()
     e0.record(stream)
     for lev, (f, g) in enumerate(host):
         ctx._check(lib.mbg_set_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
-    if form == "fp64":
-        for _ in range(steps):
-            ctx.step(1)
-            ctx._check(lib.mbg_eb_forces(ctx.h, C.cast(forces.data_ptr(), dp)), "forces")
-    else:
-        ctx.step(steps)
+    for _ in range(steps):
+        ctx.step(1)
+        result()
     for lev, (f, g) in enumerate(host):
         ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
     e1.record(stream)
@@ -204,7 +214,7 @@ def run_form(form, steps, warmup, device_index):
     state_bytes = sum(2 * f.numel() * 8 for f, _ in host)
     res["e2e"] = {"value": cups * steps / wall / 1e6, "unit": "MLUPS",
                   "h2d_bytes_per_step": state_bytes / steps,
-                  "d2h_bytes_per_step": state_bytes / steps + (24 if form == "fp64" else 0),
+                  "d2h_bytes_per_step": state_bytes / steps + (24 if form == "fp64" else 40),
                   "wall_s": wall, "device_ms": e0.elapsed_time(e1)}
     finite = True
     for lev, (f, g) in enumerate(host):
@@ -286,7 +296,10 @@ def run_batch(form, steps, warmup, device_index, count=256):
         out.update({"form": form, "ms_per_step": ms / steps, "mlups": nv * steps / (ms * 1e-3) / 1e6,
                     "gpu_launches": b.launch_count() - n0, "tuning": b.tuning(), "clocks": clk.summary(),
                     "cells": nv})
-        # end to end: upload of the initial state, the steps, download of the state
+        # end to end: upload of the initial state, the steps, download of the
+        # state (after one untimed download: the upload was warmed at setup)
+        b._check(lib.mbg_batch_get_state(b.h, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+        b._check(lib.mbg_batch_set_state(b.h, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
         b.synchronize()
         t0 = time.perf_counter()
         b._check(lib.mbg_batch_set_state(b.h, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
