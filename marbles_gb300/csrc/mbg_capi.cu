@@ -60,6 +60,13 @@ struct Level {
     long long ncoal1 = 0;
     CoalesceCell* d_coal0 = nullptr;
     long long ncoal0 = 0;
+    // FP64 explosion plan and scratch (fine levels)
+    int* d_xslot = nullptr;
+    XSlot* d_xc = nullptr;
+    long long nx = 0;
+    int* d_xix = nullptr;
+    double* d_xs = nullptr;
+    double* d_xal = nullptr;
     int cur = 0;
     double dt = 1.0;
     double dx[3], idx[3];
@@ -238,6 +245,12 @@ static void refresh_plan(mbg_ctx* ctx, Level& L)
     L.plan.nghost_cells = L.nghost;
     L.plan.ghost_list1 = L.d_ghost1;
     L.plan.nghost1 = L.nghost1;
+    L.plan.xslot = L.d_xslot;
+    L.plan.xc = L.d_xc;
+    L.plan.nx = L.nx;
+    L.plan.xix = L.d_xix;
+    L.plan.xs = L.d_xs;
+    L.plan.xal = L.d_xal;
 }
 
 extern "C" {
@@ -451,6 +464,8 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     }
     // coarse-fine ghost shell of fine levels
     std::vector<GhostCell> ghosts, ghosts1;
+    std::vector<XSlot> xcells;   // FP64 explosion plan (staging for the copies below)
+    std::vector<int> xslot;
     if (lev > 0) {
         Level& C = ctx->lv[lev - 1];
         long long goff = 0;
@@ -608,6 +623,26 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
             if ((st = dalloc(ctx, &L.gqc, (size_t)L.NG * 3)) != MBG_OK) return st;
             MBG_CUDA(cudaMemsetAsync(L.gqc, 0, (size_t)L.NG * 3 * sizeof(double), ctx->s));
         }
+        if (!ghosts.empty()) {
+            // the plan keeps coarse storage indices in 32 bits
+            if (ctx->lv[lev - 1].N >= (1LL << 31))
+                return fail(ctx, MBG_EINVAL, "mbg_define_level: coarse level holds more than 2^31 cells");
+            LevelHost h{};
+            for (int d = 0; d < 3; ++d) {
+                h.dlo[d] = L.dlo[d];
+                h.dhi[d] = L.dhi[d];
+                h.per[d] = p.is_periodic[d];
+            }
+            explode_plan(L.hbox, ghosts, h, xcells, xslot);
+            L.nx = (long long)xcells.size();
+            if ((st = dalloc(ctx, &L.d_xslot, xslot.size())) != MBG_OK) return st;
+            if ((st = dalloc(ctx, &L.d_xc, xcells.size())) != MBG_OK) return st;
+            if ((st = dalloc(ctx, &L.d_xix, (size_t)L.nx * 7)) != MBG_OK) return st;
+            if ((st = dalloc(ctx, &L.d_xs, (size_t)L.nx * 8 * NQ)) != MBG_OK) return st;
+            if ((st = dalloc(ctx, &L.d_xal, (size_t)L.nx * 6)) != MBG_OK) return st;
+            MBG_CUDA(cudaMemcpyAsync(L.d_xslot, xslot.data(), xslot.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
+            MBG_CUDA(cudaMemcpyAsync(L.d_xc, xcells.data(), xcells.size() * sizeof(XSlot), cudaMemcpyHostToDevice, ctx->s));
+        }
     }
     // the host staging vectors above must outlive their copies
     MBG_CUDA(cudaStreamSynchronize(ctx->s));
@@ -722,7 +757,7 @@ static mbg_status explode(mbg_ctx* ctx, int lev)
     } else {
         timed(ctx, TK_EXPLODE,
               [&] { launch_explode(F.plan, C.plan, C.f[C.cur], C.g[C.cur], F.fg[F.cur], F.gg[F.cur], ctx->s); });
-        ctx->launches++;
+        ctx->launches += F.plan.nx > 0 ? 3 : 0;
     }
     MBG_CUDA(cudaGetLastError());
     return MBG_OK;

@@ -24,11 +24,66 @@ __device__ __forceinline__ long long crse_index(const LV& C, const int p0[3], in
     return O.voff + val_lin(O, p[0] - O.lo[0], p[1] - O.lo[1], p[2] - O.lo[2]);
 }
 
-// One thread per fine ghost cell (neighbouring threads read neighbouring
-// coarse cells, so each component's loads coalesce); the seven coarse cells
-// of the stencil are located once, then every component is read from them.
-__global__ void k_explode(LV F, LV C, const GhostCell* gl, long long n, const double* fc, const double* gc_,
-                          double* fg, double* gg)
+// The slopes and the limiter depend only on the coarse cell, so they are
+// computed once per coarse cell under the ghost shell (a slot), not once per
+// fine child; each child then evaluates the same expression as before.
+//
+// 1. the 7 coarse storage indices of each slot (centre, -/+ x, y, z; -1 where
+//    no coarse box holds the cell); limiter reset to 1
+__global__ void k_xindex(LV C, const XSlot* __restrict__ xc, long long nx, int* __restrict__ ix,
+                         double* __restrict__ al)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nx) return;
+    const XSlot c = xc[e];
+    const int cp[3] = {c.x, c.y, c.z};
+    ix[e] = (int)crse_index(C, cp, 0, 0);
+    for (int d = 0; d < 3; ++d) {
+        ix[(1 + 2 * d) * nx + e] = (int)crse_index(C, cp, d, -1);
+        ix[(2 + 2 * d) * nx + e] = (int)crse_index(C, cp, d, 1);
+    }
+    for (int k = 0; k < 6; ++k) al[k * nx + e] = 1.0;
+}
+
+// 2. per (slot, direction): value, centred slopes, and each axis' limiter
+//    ratio folded into the slot's minimum (non-negative doubles order like
+//    their bit patterns, so an integer atomicMin is exact and order-free,
+//    as fmin is)
+__global__ void k_xslope(LV C, const int* __restrict__ ix, long long nx, const double* __restrict__ fc,
+                         const double* __restrict__ gc_, double* __restrict__ xs, double* __restrict__ al)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    if (e >= nx) return;
+    int id[7];
+    for (int k = 0; k < 7; ++k) id[k] = ix[k * nx + e];
+    for (int lat = 0; lat < 2; ++lat) {
+        const double* __restrict__ v = (lat ? gc_ : fc) + (long long)q * C.N;
+        double u[7];
+        for (int k = 0; k < 7; ++k) u[k] = id[k] >= 0 ? v[id[k]] : 0.0;
+        double* o = xs + ((long long)(lat * 4) * NQ + q) * nx + e;
+        o[0] = u[0];
+        for (int d = 0; d < 3; ++d) {
+            const double u0 = u[0], um = u[1 + 2 * d], up = u[2 + 2 * d];
+            const double cen = 0.5 * (up - um);
+            const double forw = 2.0 * (up - u0);
+            const double back = 2.0 * (u0 - um);
+            const double slp = (forw * back >= 0.0) ? fmin(fabs(forw), fabs(back)) : 0.0;
+            o[(long long)(1 + d) * NQ * nx] = cen;
+            if (cen != 0.0) {
+                const double r = fmin(slp, fabs(cen)) / fabs(cen);
+                if (r < 1.0)
+                    atomicMin((unsigned long long*)&al[(lat * 3 + d) * nx + e],
+                              (unsigned long long)__double_as_longlong(r));
+            }
+        }
+    }
+}
+
+// 3. one thread per fine ghost cell: u0 + sum_d off_d (alpha_d slope_d)
+__global__ void k_xfill(LV F, const GhostCell* __restrict__ gl, const int* __restrict__ slot, long long n,
+                        const double* __restrict__ xs, const double* __restrict__ al, long long nx,
+                        double* __restrict__ fg, double* __restrict__ gg)
 {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
@@ -40,38 +95,18 @@ __global__ void k_explode(LV F, LV C, const GhostCell* gl, long long n, const do
     const double off[3] = {((fp[0] - 2 * cp[0]) + 0.5) / 2.0 - 0.5, ((fp[1] - 2 * cp[1]) + 0.5) / 2.0 - 0.5,
                            ((fp[2] - 2 * cp[2]) + 0.5) / 2.0 - 0.5};
     const long long gi = B.goff + fab_lin(B, g.x, g.y, g.z);
-    // centre, then -/+ along x, y, z
-    long long ix[7];
-    ix[0] = crse_index(C, cp, 0, 0);
-    for (int d = 0; d < 3; ++d) {
-        ix[1 + 2 * d] = crse_index(C, cp, d, -1);
-        ix[2 + 2 * d] = crse_index(C, cp, d, 1);
-    }
+    const long long sl = slot[e];
     for (int lat = 0; lat < 2; ++lat) {
-        const double* v = lat ? gc_ : fc;
-        double* out = lat ? gg : fg;
-        auto at = [&](int k, int q) { return ix[k] >= 0 ? v[q * C.N + ix[k]] : 0.0; };
-        // limiter factors: directions outermost, the seven stencil values of
-        // each read once (fmin is exact, so the order of the minimum is free)
-        double alpha[3] = {1.0, 1.0, 1.0};
+        double* __restrict__ out = lat ? gg : fg;
+        const double a0 = al[(lat * 3 + 0) * nx + sl], a1 = al[(lat * 3 + 1) * nx + sl],
+                     a2 = al[(lat * 3 + 2) * nx + sl];
+        const double* __restrict__ x = xs + (long long)(lat * 4) * NQ * nx + sl;
         for (int q = 0; q < NQ; ++q) {
-            double u[7];
-            for (int k = 0; k < 7; ++k) u[k] = at(k, q);
-            for (int d = 0; d < 3; ++d) {
-                const double u0 = u[0], um = u[1 + 2 * d], up = u[2 + 2 * d];
-                const double cen = 0.5 * (up - um);
-                const double forw = 2.0 * (up - u0);
-                const double back = 2.0 * (u0 - um);
-                const double slp = (forw * back >= 0.0) ? fmin(fabs(forw), fabs(back)) : 0.0;
-                if (cen != 0.0) alpha[d] = fmin(alpha[d], fmin(slp, fabs(cen)) / fabs(cen));
-            }
-        }
-        for (int q = 0; q < NQ; ++q) {
-            const double u0 = at(0, q);
-            const double cx = 0.5 * (at(2, q) - at(1, q));
-            const double cy = 0.5 * (at(4, q) - at(3, q));
-            const double cz = 0.5 * (at(6, q) - at(5, q));
-            out[q * F.NG + gi] = u0 + off[0] * (alpha[0] * cx) + off[1] * (alpha[1] * cy) + off[2] * (alpha[2] * cz);
+            const double u0 = x[(long long)q * nx];
+            const double cx = x[(long long)(NQ + q) * nx];
+            const double cy = x[(long long)(2 * NQ + q) * nx];
+            const double cz = x[(long long)(3 * NQ + q) * nx];
+            out[q * F.NG + gi] = u0 + off[0] * (a0 * cx) + off[1] * (a1 * cy) + off[2] * (a2 * cz);
         }
     }
 }
@@ -131,11 +166,12 @@ __global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, const CoalesceCell
 void launch_explode(const LevelPlan& fine, const LevelPlan& crse, const double* fc, const double* gc, double* fg,
                     double* gg, cudaStream_t s)
 {
-    if (fine.nghost_cells == 0) return;
-    const int th = 128;
-    const long long nb = (fine.nghost_cells + th - 1) / th;
-    k_explode<<<(unsigned)nb, th, 0, s>>>(fine.view64, crse.view64, fine.ghost_list, fine.nghost_cells, fc, gc, fg,
-                                          gg);
+    if (fine.nghost_cells == 0 || fine.nx == 0) return;
+    const unsigned bx = (unsigned)((fine.nx + 127) / 128);
+    k_xindex<<<bx, 128, 0, s>>>(crse.view64, fine.xc, fine.nx, fine.xix, fine.xal);
+    k_xslope<<<dim3(bx, NQ), 128, 0, s>>>(crse.view64, fine.xix, fine.nx, fc, gc, fine.xs, fine.xal);
+    k_xfill<<<(unsigned)((fine.nghost_cells + 127) / 128), 128, 0, s>>>(
+        fine.view64, fine.ghost_list, fine.xslot, fine.nghost_cells, fine.xs, fine.xal, fine.nx, fg, gg);
 }
 
 void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParams& P, const Phys64& ph,

@@ -29,6 +29,12 @@ struct GhostCell {
     short layer;     // Chebyshev distance to the box
 };
 
+// a coarse cell under a fine level's uncovered ghost shell (global coarse
+// coordinates): the explosion computes its slopes and limiter once
+struct XSlot {
+    int x, y, z, pad;
+};
+
 struct CoalesceCell {
     int cbox;             // coarse box holding the cell
     int fbox;             // fine box whose average is kept (last writer)
@@ -61,6 +67,15 @@ struct LevelPlan {
     long long nghost_cells = 0;
     const GhostCell* ghost_list1 = nullptr;  // first ghost layer only
     long long nghost1 = 0;
+    // FP64 explosion: each ghost cell's slot, the slots' coarse cells, and per
+    // slot the 7 coarse storage indices [7][nx], value and centred slopes
+    // [lattice][4][NQ][nx], limiter [lattice][3][nx]
+    const int* xslot = nullptr;
+    const XSlot* xc = nullptr;
+    long long nx = 0;
+    int* xix = nullptr;
+    double* xs = nullptr;
+    double* xal = nullptr;
 };
 
 // FP64 form (mbg_fp64.cu)

@@ -318,8 +318,8 @@ static void ghost_plan(const std::vector<DevBox>& box, const std::vector<GhostCe
 // explosion plan: the distinct coarse cells under the uncovered ghost cells,
 // numbered in order of first use so that neighbouring ghost cells read
 // neighbouring slots
-static void explode_plan(const std::vector<DevBox>& box, const std::vector<GhostCell>& ghosts, const LevelHost& h,
-                         std::vector<XSlot>& xc, std::vector<int>& slot)
+void explode_plan(const std::vector<DevBox>& box, const std::vector<GhostCell>& ghosts, const LevelHost& h,
+                  std::vector<XSlot>& xc, std::vector<int>& slot)
 {
     auto floor2 = [](int v) { return v >= 0 ? v / 2 : -((1 - v) / 2); };
     std::unordered_map<long long, int> id;

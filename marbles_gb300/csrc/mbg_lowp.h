@@ -34,6 +34,11 @@ struct LevelHost {
     int dlo[3], dhi[3], G[3], nb[3], per[3];
 };
 
+// the explosion's slots: the distinct coarse cells under a fine level's
+// uncovered ghost cells, numbered in order of first use, and each ghost cell's
+// slot (shared by both forms)
+void explode_plan(const std::vector<DevBox>& box, const std::vector<GhostCell>& ghosts, const LevelHost& h,
+                  std::vector<XSlot>& xc, std::vector<int>& slot);
 mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::vector<DevBox>& hbox, long long N,
                        long long NG, double dt, const double idx[3], const LevelHost& host, LowpLevel& L,
                        std::string& err);

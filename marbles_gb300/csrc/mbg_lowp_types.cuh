@@ -48,12 +48,9 @@ struct HaloCell {
 };
 
 // explosion plan of a fine level: the distinct coarse cells under its
-// uncovered ghost cells (global coarse coordinates), each ghost cell's slot
-// among them, and per-slot scratch: the 7 coarse neighbours' storage indices
-// [7][nx], value and centred slopes [lattice][4][NQ][nx], limiter [lattice][3][nx]
-struct XSlot {
-    int x, y, z, pad;
-};
+// uncovered ghost cells (XSlot), each ghost cell's slot among them, and
+// per-slot scratch: the 7 coarse neighbours' storage indices [7][nx], value
+// and centred slopes [lattice][4][NQ][nx], limiter [lattice][3][nx]
 struct ExplodePlan {
     const GhostCell* gl;
     const int* slot;
