@@ -43,6 +43,8 @@ WORKLOADS = {
     "sphere256": dict(kind="sphere"),
 }
 _WL = ["pulse128"]
+# timed repetitions of the end-to-end sequence (median reported)
+E2E_REPEATS = 3
 
 
 def inputs_text():
@@ -186,7 +188,11 @@ def run_form(form, steps, warmup, device_index):
     # the EB force, which the reference computes every step; 16-bit: the FP64
     # conservation totals), download of the state.  One untimed round first:
     # the first copies from freshly pinned buffers pay a one-time mapping cost
-    # (about 0.1 s on the GB300 machine), as the first steps pay for warm-up.
+    # (about 0.1 s on the GB300 machine), as the first steps pay for warm-up.  On
+    # the GB300 machine single state copies still stalled for 70-130 ms now and
+    # then within the first two rounds, so the whole timed sequence runs
+    # E2E_REPEATS times and the median wall time is reported, all of them
+    # listed beside it.
     res_buf = torch.zeros(5, dtype=torch.float64, pin_memory=True)
     rb = C.cast(res_buf.data_ptr(), dp)
 
@@ -199,23 +205,28 @@ def run_form(form, steps, warmup, device_index):
         ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
     result()
     ctx.synchronize()
-    t0 = time.perf_counter()
-    e0.record(stream)
-    for lev, (f, g) in enumerate(host):
-        ctx._check(lib.mbg_set_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
-    for _ in range(steps):
-        ctx.step(1)
-        result()
-    for lev, (f, g) in enumerate(host):
-        ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
-    e1.record(stream)
-    e1.synchronize()
-    wall = time.perf_counter() - t0
+    walls, dev_ms = [], []
+    for _ in range(E2E_REPEATS):
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for lev, (f, g) in enumerate(host):
+            ctx._check(lib.mbg_set_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
+        for _ in range(steps):
+            ctx.step(1)
+            result()
+        for lev, (f, g) in enumerate(host):
+            ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+        e1.record(stream)
+        e1.synchronize()
+        walls.append(time.perf_counter() - t0)
+        dev_ms.append(e0.elapsed_time(e1))
+    k = sorted(range(len(walls)), key=lambda i: walls[i])[len(walls) // 2]
+    wall = walls[k]
     state_bytes = sum(2 * f.numel() * 8 for f, _ in host)
     res["e2e"] = {"value": cups * steps / wall / 1e6, "unit": "MLUPS",
                   "h2d_bytes_per_step": state_bytes / steps,
                   "d2h_bytes_per_step": state_bytes / steps + (24 if form == "fp64" else 40),
-                  "wall_s": wall, "device_ms": e0.elapsed_time(e1)}
+                  "wall_s": wall, "device_ms": dev_ms[k], "repeats_wall_s": walls}
     finite = True
     for lev, (f, g) in enumerate(host):
         finite &= bool(torch.isfinite(f).all()) and bool(torch.isfinite(g).all())

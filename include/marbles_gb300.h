@@ -154,8 +154,10 @@ mbg_status mbg_average_down(mbg_ctx* ctx, int crse_lev, int crse_ng);
 mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3]);
 
 /* Conserved totals of the stored state over all levels, each cell counted on
- * the finest level that holds it and weighted by its volume, accumulated in
- * FP64 on the device (both forms): out = {mass, momentum x, y, z, sum of
+ * the finest level that holds it and weighted by its volume, summed on the
+ * device (FP64 form: FP64 throughout; 16-bit forms: each cell's 27 decoded
+ * FP32 values in error-free FP32 TwoSum arithmetic, about 2^-48 relative,
+ * then FP64 across cells): out = {mass, momentum x, y, z, sum of
  * 2 rho E}.  No counterpart in the reference (its only global reduction is
  * the EB-force sum, Source/LBM.cpp:1040); one reduction launch per level. */
 mbg_status mbg_conserved(mbg_ctx* ctx, double out[5]);

@@ -1020,8 +1020,28 @@ __global__ void k_macro16(const LowpK* __restrict__ K, const CodecTab ct, const 
     for (int k = 0; k < 19; ++k) o[k * vol] = vals[k];
 }
 
-// conserved totals of the decoded stored state, FP64 accumulation (as
-// mbg_fp64_out.cu::k_conserved)
+// running FP32 sum carried as hi + lo: TwoSum (Knuth, TAOCP vol. 2,
+// 4.2.2) gives the rounding error of each addition exactly, and lo collects
+// those errors, so hi + lo holds the sum to about 2^-48 relative.  The
+// explicit-rounding intrinsics keep the compiler from contracting or
+// reordering the error terms.
+struct Sum2f {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float b)
+    {
+        const float s = __fadd_rn(hi, b);
+        const float bb = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+        hi = s;
+        lo = __fadd_rn(lo, e);
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// conserved totals of the decoded stored state (the quantities of
+// mbg_fp64_out.cu::k_conserved): the per-cell sums of the 27 decoded FP32
+// values in FP32 TwoSum arithmetic (GB300's FP64 pipe made the FP64 per-cell
+// sums the kernel's bound), the cross-cell sums in FP64
 template <bool BF>
 __global__ void __launch_bounds__(TILE_CELLS) k_conserved16(const LowpK* __restrict__ K, const Tile* tiles, double dV,
                                                             double* out5)
@@ -1036,18 +1056,25 @@ __global__ void __launch_bounds__(TILE_CELLS) k_conserved16(const LowpK* __restr
         const uint8_t tf = flag_at(L, B, x, y, z);
         if ((tf & FL_FLUID) && !(tf & FL_COV)) {
             const long long cell = B.voff + val_lin(B, x, y, z);
-            MomentAcc<double> acc;
-#define MBG_CN16(q)                                                                                     \
-    acc.template add<q>((double)dec<BF>(K->ct, K->s.f[q * L.N + cell], q, false),                       \
-                        (double)dec<BF>(K->ct, K->s.g[q * L.N + cell], q, true));
+            Sum2f rho, mu, mv, mw, tre;
+#define MBG_CN16(q)                                                                           \
+    {                                                                                         \
+        constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);                               \
+        const float fq = dec<BF>(K->ct, K->s.f[q * L.N + cell], q, false);                    \
+        rho.add(fq);                                                                          \
+        if constexpr (ex != 0) mu.add(ex > 0 ? fq : -fq);                                     \
+        if constexpr (ey != 0) mv.add(ey > 0 ? fq : -fq);                                     \
+        if constexpr (ez != 0) mw.add(ez > 0 ? fq : -fq);                                     \
+        tre.add(dec<BF>(K->ct, K->s.g[q * L.N + cell], q, true));                             \
+    }
             MBG_UNROLL27(MBG_CN16)
 #undef MBG_CN16
             const double ms = K->ph.mesh_speed;
-            v[0] = acc.rho * dV;
-            v[1] = acc.u * ms * dV;
-            v[2] = acc.v * ms * dV;
-            v[3] = acc.w * ms * dV;
-            v[4] = acc.tre * dV;
+            v[0] = rho.value() * dV;
+            v[1] = mu.value() * ms * dV;
+            v[2] = mv.value() * ms * dV;
+            v[3] = mw.value() * ms * dV;
+            v[4] = tre.value() * dV;
         }
     }
     const int t = threadIdx.x;
