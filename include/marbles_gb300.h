@@ -261,16 +261,18 @@ void mbg_adj_destroy(mbg_adj* a);
  * cudaMalloc / cudaFree may synchronise the device, which a caller queueing
  * its time loop asynchronously on its own stream cannot accept.
  *
- * One FP64 step (stream, collide, relax: the reference's LBM::advance) of a
- * single all-fluid box that is periodic in every direction, of
- * params->n_cell cells (at most MBG_NOALLOC_MAX_CELLS in total), with no
- * context and no allocation.  f_in, g_in, f_out, g_out are device arrays of
- * 27 * ncells doubles in [q][k][j][i] order; outputs must not alias inputs.
- * The scratch between the two passes is a fixed array in the library's
- * device image (4.5 MiB on every GPU that loads the library, until exit),
- * shared by all calls: calls whose kernels overlap on the GPU race on it.
- * The first call on a device looks up that array's address (with the
- * device current) and should come before any stream capture.  Launches on
+ * One FP64 step (stream, then collide and relax) of a single all-fluid box
+ * that is periodic in every direction, of params->n_cell cells (at most
+ * MBG_NOALLOC_MAX_CELLS in total), with no context and no allocation.
+ * f_in, g_in, f_out, g_out are device arrays of 27 * ncells doubles in
+ * [q][k][j][i] order; outputs must not alias inputs.  The scratch between
+ * the two passes is a fixed array in the library's device image (4.5 MiB on
+ * every GPU that loads the library, until exit), shared by all calls: calls
+ * whose kernels overlap on the GPU race on it.  Each call looks up that
+ * array's address on the current device (a host-side lookup, no device
+ * work); the first call on a device may load the library's device code and
+ * should come before any stream capture.  A box with any n_cell[d], or the
+ * product, above the maximum is rejected with MBG_EINVAL.  Launches on
  * cuda_stream (NULL: the legacy default stream); errors are reported by
  * mbg_last_error(NULL). */
 #define MBG_NOALLOC_MAX_CELLS 32768

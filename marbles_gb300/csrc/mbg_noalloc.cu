@@ -18,11 +18,12 @@
 // the caller.  Each call rewrites every scratch entry it later reads, so
 // nothing needs clearing between calls.
 //
-// The first call on a device looks up the array's device address with that
-// device current (cudaGetSymbolAddress) and caches it; make that first call
-// outside any stream capture.
+// Every call looks up the array's device address on the current device
+// (cudaGetSymbolAddress, a host-side lookup with no device work) instead of
+// caching it, so that a context torn down and re-created by cudaDeviceReset
+// never leaves a stale address behind.  The first call on a device may load
+// the library's device code; make that first call outside any stream capture.
 #include <cstdio>
-#include <mutex>
 #include <string>
 
 #include "../../include/marbles_gb300.h"
@@ -182,9 +183,6 @@ using namespace mbg;
 void mbg_set_global_error(const std::string& msg);
 
 namespace {
-std::mutex g_na_mutex;
-void* g_na_ptr[64] = {nullptr};
-
 mbg_status na_fail(const std::string& m)
 {
     mbg_set_global_error("mbg_step_box_noalloc: " + m);
@@ -202,6 +200,12 @@ extern "C" mbg_status mbg_step_box_noalloc(const mbg_params* p, const double* f_
         if (p->n_cell[d] < 1) return na_fail("n_cell must be positive");
         if (!(p->prob_hi[d] > p->prob_lo[d])) return na_fail("prob_hi must exceed prob_lo");
     }
+    // each factor is checked before the product is formed, so the product
+    // cannot overflow (every n_cell[d] <= the maximum, itself < 2^21)
+    for (int d = 0; d < 3; ++d)
+        if (p->n_cell[d] > NOALLOC_MAX_CELLS)
+            return na_fail("n_cell[" + std::to_string(d) + "] = " + std::to_string(p->n_cell[d]) +
+                           " exceeds the maximum of " + std::to_string(NOALLOC_MAX_CELLS) + " cells");
     const long long N = (long long)p->n_cell[0] * p->n_cell[1] * p->n_cell[2];
     if (N > NOALLOC_MAX_CELLS)
         return na_fail("box of " + std::to_string(N) + " cells exceeds the maximum of " +
@@ -210,27 +214,14 @@ extern "C" mbg_status mbg_step_box_noalloc(const mbg_params* p, const double* f_
         return na_fail("nu, alpha, dt_outer, m_bar must be positive and adiabatic_exponent > 1");
     if (f_out == f_in || f_out == g_in || g_out == f_in || g_out == g_in || f_out == g_out)
         return na_fail("outputs must not alias inputs or each other");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        mbg_set_global_error(std::string("mbg_step_box_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
-        return MBG_ECUDA;
-    }
-    if (dev < 0 || dev >= 64) return na_fail("device index out of range");
+    // the scratch array's address on the current device, looked up on every
+    // call (a cached address would go stale after cudaDeviceReset)
     void* scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_na_mutex);
-        if (!g_na_ptr[dev]) {
-            void* ptr = nullptr;
-            e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_scratch);
-            if (e != cudaSuccess || !ptr) {
-                mbg_set_global_error(std::string("mbg_step_box_noalloc: cudaGetSymbolAddress: ") +
-                                     cudaGetErrorString(e));
-                return MBG_ECUDA;
-            }
-            g_na_ptr[dev] = ptr;
-        }
-        scratch = g_na_ptr[dev];
+    cudaError_t e = cudaGetSymbolAddress(&scratch, g_noalloc_scratch);
+    if (e != cudaSuccess || !scratch) {
+        mbg_set_global_error(std::string("mbg_step_box_noalloc: cudaGetSymbolAddress: ") +
+                             cudaGetErrorString(e));
+        return MBG_ECUDA;
     }
     BoxDims b;
     for (int d = 0; d < 3; ++d) b.n[d] = p->n_cell[d];

@@ -638,6 +638,20 @@ struct Sim {
         }
     }
 
+    // IC.H:474-519 for one cell: f = f_eq(rho, u, R T), g = Grad g_eq
+    static void equilibrium_cell(double rho, const double vel[3], double temp, double Rg, double gamma,
+                                 double* f, double* g)
+    {
+        const double cv_ = Rg / (gamma - 1.0);
+        const double two_rho_e = get_energy(temp, rho, vel, cv_);
+        double qeq[3], req[6];
+        get_equilibrium_moments(rho, vel, two_rho_e, cv_, Rg, qeq, req);
+        for (int q = 0; q < NQ; ++q) {
+            f[q] = set_equilibrium_value(rho, vel, Rg * temp, q);
+            g[q] = grad_expansion(two_rho_e, qeq, req, q);
+        }
+    }
+
     // IC.H:474-519 over the grown boxes
     void initialize_f(int lev)
     {
@@ -653,13 +667,11 @@ struct Sim {
                     for (int i = gb.lo[0]; i <= gb.hi[0]; ++i) {
                         double rho = 1.0, vel[3] = {0, 0, 0}, temp = 1.0 / 3.0, Rg = 1.0, gamma = 1.667;
                         ic_state(L, i, j, k, rho, vel, temp, Rg, gamma);
-                        const double cv_ = Rg / (gamma - 1.0);
-                        const double two_rho_e = get_energy(temp, rho, vel, cv_);
-                        double qeq[3], req[6];
-                        get_equilibrium_moments(rho, vel, two_rho_e, cv_, Rg, qeq, req);
+                        double fe[NQ], ge[NQ];
+                        equilibrium_cell(rho, vel, temp, Rg, gamma, fe, ge);
                         for (int q = 0; q < NQ; ++q) {
-                            F(i, j, k, q) = set_equilibrium_value(rho, vel, Rg * temp, q);
-                            Gf(i, j, k, q) = grad_expansion(two_rho_e, qeq, req, q);
+                            F(i, j, k, q) = fe[q];
+                            Gf(i, j, k, q) = ge[q];
                         }
                     }
         }
@@ -860,18 +872,54 @@ struct Sim {
                 for (int j = vb.lo[1]; j <= vb.hi[1]; ++j)
                     for (int i = vb.lo[0]; i <= vb.hi[0]; ++i) {
                         if (a(i, j, k, 0) != 1) continue;
-                        double feq[NQ], geq[NQ];
-                        cell_equilibrium(M, D, i, j, k, nu, alpha, dt, feq, geq);
-                        const double temperature = M(i, j, k, TEMP);
-                        const double omega = 1.0 / (nu / (R * temperature * dt) + 0.5);
-                        for (int q = 0; q < NQ; ++q) {
-                            F(i, j, k, q) += omega * (feq[q] - F(i, j, k, q));
-                            Gf(i, j, k, q) += omega * (geq[q] - Gf(i, j, k, q));
-                        }
+                        relax_cell(M, D, i, j, k, nu, alpha, dt, F, Gf);
                     }
         }
         fill_boundary(L, L.f, NG);
         fill_boundary(L, L.g, NG);
+    }
+
+    // LBM.cpp:765-807 for one cell: f += omega (f_eq - f), g likewise
+    void relax_cell(const DFab& M, const DFab& D, int i, int j, int k, double nu, double alpha, double dt,
+                    DFab& F, DFab& Gf) const
+    {
+        double feq[NQ], geq[NQ];
+        cell_equilibrium(M, D, i, j, k, nu, alpha, dt, feq, geq);
+        const double temperature = M(i, j, k, TEMP);
+        const double omega = 1.0 / (nu / (R * temperature * dt) + 0.5);
+        for (int q = 0; q < NQ; ++q) {
+            F(i, j, k, q) += omega * (feq[q] - F(i, j, k, q));
+            Gf(i, j, k, q) += omega * (geq[q] - Gf(i, j, k, q));
+        }
+    }
+
+    // The collision of one cell in isolation: post-stream f, g and the
+    // q-correction gradient dq in, post-collision f, g and the cell's Q_corr
+    // out (f_to_macrodata, macrodata_to_equilibrium and relax of
+    // LBM.cpp:621-906 with the gradient supplied instead of taken from the
+    // neighbours).  Used by the linear-stability analysis of the scheme.
+    void collide_cell(const double* f, const double* g, const double* dq, double dt, double* fo, double* go,
+                      double* qc) const
+    {
+        IBox b;
+        for (int d = 0; d < 3; ++d) { b.lo[d] = 0; b.hi[d] = 0; }
+        DFab F, Gf, M, D;
+        F.define(b, NQ, 0.0);
+        Gf.define(b, NQ, 0.0);
+        M.define(b, NMAC, 0.0);
+        D.define(b, NDER, 0.0);
+        for (int q = 0; q < NQ; ++q) { F(0, 0, 0, q) = f[q]; Gf(0, 0, 0, q) = g[q]; }
+        double m[NMAC];
+        cell_macro(F, Gf, 0, 0, 0, mesh_speed, m);
+        for (int c = 0; c < NMAC; ++c) M(0, 0, 0, c) = m[c];
+        D(0, 0, 0, DQX) = dq[0];
+        D(0, 0, 0, DQY) = dq[1];
+        D(0, 0, 0, DQZ) = dq[2];
+        relax_cell(M, D, 0, 0, 0, p.nu, p.alpha, dt, F, Gf);
+        for (int q = 0; q < NQ; ++q) { fo[q] = F(0, 0, 0, q); go[q] = Gf(0, 0, 0, q); }
+        qc[0] = m[QCX];
+        qc[1] = m[QCY];
+        qc[2] = m[QCZ];
     }
 
     void cell_equilibrium(const DFab& M, const DFab& D, int i, int j, int k, double nu, double alpha,
@@ -1473,6 +1521,23 @@ int orc_get_grown_flags(void* h, int lev, unsigned char* out)
                 for (int i = gb.lo[0]; i <= gb.hi[0]; ++i)
                     out[off++] = (unsigned char)((a(i, j, k, 0) & 1) | ((a(i, j, k, 1) & 1) << 1));
     }
+    return 0;
+}
+
+// equilibrium populations of one cell at (rho, vel, T) with the simulation's
+// gas constant and adiabatic exponent (the initializer's f_eq and g_eq)
+int orc_equilibrium_cell(void* h, double rho, const double* vel, double temp, double* f, double* g)
+{
+    auto* s = static_cast<Sim*>(h);
+    Sim::equilibrium_cell(rho, vel, temp, s->R, s->p.adiabatic_exponent, f, g);
+    return 0;
+}
+
+// collision of one cell with a given q-correction gradient (see collide_cell)
+int orc_collide_cell(void* h, const double* f, const double* g, const double* dq, double dt, double* fo,
+                     double* go, double* qc)
+{
+    static_cast<Sim*>(h)->collide_cell(f, g, dq, dt, fo, go, qc);
     return 0;
 }
 

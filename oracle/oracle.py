@@ -90,6 +90,8 @@ def lib():
         L.orc_stencil.argtypes = [ip, dp, ip, ip, ip, ip]
         L.orc_get_grown_flags.argtypes = [vp, C.c_int, C.POINTER(C.c_uint8)]
         L.orc_eb_forces.argtypes = [vp, dp]
+        L.orc_equilibrium_cell.argtypes = [vp, C.c_double, dp, C.c_double, dp, dp]
+        L.orc_collide_cell.argtypes = [vp, dp, dp, dp, C.c_double, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -180,6 +182,10 @@ class Oracle:
     def step(self, n=1):
         self.L.orc_step(self.h, n)
 
+    def advance_level(self, lev):
+        """One advance of level lev in isolation (stream f, g + collide)."""
+        self.L.orc_advance_level(self.h, lev)
+
     def average_down(self, crse_lev, ng):
         self.L.orc_average_down(self.h, crse_lev, ng)
 
@@ -221,6 +227,26 @@ class Oracle:
         out = np.zeros(3)
         self.L.orc_eb_forces(self.h, _dp(out))
         return out
+
+    def equilibrium_cell(self, rho, vel, temp):
+        """f_eq, g_eq of one cell at (rho, vel, T) (the initializer's)."""
+        v = np.ascontiguousarray(vel, dtype=np.float64)
+        f = np.empty(NQ)
+        g = np.empty(NQ)
+        self.L.orc_equilibrium_cell(self.h, rho, _dp(v), temp, _dp(f), _dp(g))
+        return f, g
+
+    def collide_cell(self, f, g, dq, dt=1.0):
+        """One cell's collision with the q-correction gradient dq supplied:
+        returns post-collision f, g and the cell's Q_corr (3 values)."""
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        g = np.ascontiguousarray(g, dtype=np.float64)
+        d = np.ascontiguousarray(dq, dtype=np.float64)
+        fo = np.empty(NQ)
+        go = np.empty(NQ)
+        qc = np.empty(3)
+        self.L.orc_collide_cell(self.h, _dp(f), _dp(g), _dp(d), dt, _dp(fo), _dp(go), _dp(qc))
+        return fo, go, qc
 
     def close(self):
         if self.h:

@@ -1,7 +1,8 @@
 """Writes the golden fixtures of tests/golden from the reference checkout.
 
-Run once where the NREL/marbles sources are present:
-    python tests/golden/make_fixtures.py /root/reference
+Run once where the NREL/marbles sources are present, giving the path of the
+checkout (required):
+    python tests/golden/make_fixtures.py <path-to-marbles-checkout>
 It reads, as text only:
   * Source/Stencil.H     -> stencil_d3q27.json: the D3Q27 direction table,
                             the four bounce tables and the weight expressions
@@ -76,7 +77,9 @@ def notebooks(ref):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_fixtures.py <path-to-marbles-checkout>")
+    ref = sys.argv[1]
     json.dump(stencil(ref), open(os.path.join(HERE, "stencil_d3q27.json"), "w"), indent=1)
     json.dump(notebooks(ref), open(os.path.join(HERE, "notebook_runs.json"), "w"), indent=1)
     print("wrote fixtures to", HERE)
