@@ -3,13 +3,22 @@
 Workload: the two-level AMR Gaussian pulse -- coarse 128^3 periodic, fine
 level (ratio 2) over the central 64^3 coarse cells (128^3 fine cells),
 max_grid_size 32, blocking factor 8, nu = 0.01, rho = 1 + 0.01 exp(-r^2 / 2 8^2),
-u = 0, T = 1/3; each coarse step advances the coarse level once and the fine
-level twice (6.29 M cell-updates).  Inputs are synthetic (analytic IC).
+u = 0, at RT = 0.1; each coarse step advances the coarse level once and the
+fine level twice (6.29 M cell-updates).  At the literal RT = 1/3 the reference
+scheme is linearly unstable at this viscosity (growth 2.2 per step,
+tests/test_stability.py) and the state overflows within the warm-up, so the
+stable RT = 0.1 variant of the same grids is timed; the arithmetic per cell
+does not depend on T.  Inputs are synthetic (analytic IC).
+
+Headline `value`: the FP64 form (the reference's storage and arithmetic,
+bit-identical to the oracle).  The FP16 and BF16 storage forms (FP32
+arithmetic) are measured on the same workload and reported under `forms`.
 
 Metric: MLUPS (million fluid cell-updates per second, fine substeps
 counted), device-timed with CUDA events on the library's stream over K
 coarse steps after W warm-up steps; the state (1.8 GB in FP64) is far larger
-than L2, so no flush is needed between steps.
+than L2, so no flush is needed between steps.  Every form's state must stay
+finite over the timed steps and the end-to-end leg, else the run exits 1.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp64|fp16|bf16|all]
   python bench.py --impl reference ...     # the CPU oracle on the host cores
@@ -31,27 +40,39 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 BYTES_PER_CELL = {"fp64": 865, "fp16": 217, "bf16": 217}   # read + write f, g, one flag byte
 PRECISION = {"fp64": 0, "fp16": 1, "bf16": 2}
 WORKLOAD = ("two-level AMR Gaussian pulse: coarse 128^3 periodic + fine 128^3 (ratio 2 over the central "
-            "64^3 coarse cells), max_grid_size 32, blocking_factor 8, nu 0.01, D3Q27 f+g")
+            "64^3 coarse cells), max_grid_size 32, blocking_factor 8, nu 0.01, RT 0.1, D3Q27 f+g")
+# the stable temperature of the timed pulse (RT = 1/3 diverges in the scheme)
+PULSE_T0 = 0.1
 
 
 WORKLOADS = {
-    "pulse128": dict(nc=128, lo=32, hi=96, mgs=32, width=8.0),
+    "pulse128": dict(nc=128, lo=32, hi=96, mgs=32, width=8.0, t0=PULSE_T0),
     # small case of the same kernels for profiler captures (226 MB FP64 state)
-    "pulse64": dict(nc=64, lo=16, hi=48, mgs=32, width=4.0),
+    "pulse64": dict(nc=64, lo=16, hi=48, mgs=32, width=4.0, t0=PULSE_T0),
     # flow past a sphere, 256 x 128 x 128, three levels around the sphere
     # (inflow at x-low, outflow at x-high, periodic in y and z, Re 100)
     "sphere256": dict(kind="sphere"),
 }
 _WL = ["pulse128"]
+# viscosity range of the timed batch (stable at RT = 1/3)
+BATCH_NU = (0.15, 0.2)
 # timed repetitions of the end-to-end sequence (median reported)
 E2E_REPEATS = 3
+
+
+# the sphere at the literal RT = 1/3 diverges like the pulse; RT = 0.03 is
+# stable (tests/test_stability.py), with the same Mach number (inflow 0.015)
+SPHERE_T0 = 0.03
 
 
 def inputs_text():
     import inputs
     w = dict(WORKLOADS[_WL[0]])
-    return inputs.sphere(**{k: v for k, v in w.items() if k != "kind"}) if w.get("kind") == "sphere" \
-        else inputs.pulse(**w)
+    if w.get("kind") == "sphere":
+        return inputs.sphere(**{k: v for k, v in w.items() if k != "kind"}) + (
+            "\nic_constant.initial_temperature = %r\nvelocity_bc_constant.initial_temperature = %r\n"
+            % (SPHERE_T0, SPHERE_T0))
+    return inputs.pulse(**w)
 
 
 def peaks():
@@ -139,16 +160,33 @@ def run_form(form, steps, warmup, device_index):
     nlev = d.num_levels()
     cups = cell_updates_per_step(d, nlev)
     stream = torch.cuda.ExternalStream(ctx.stream())
-    # the initial state in pinned host buffers (input of the end-to-end leg)
     dp = C.POINTER(C.c_double)
     lib = M.lib()
-    host = []
+
+    def pinned(n):
+        return torch.empty(n, dtype=torch.float64, pin_memory=True)
+
+    # the initial state in pinned host buffers: the input of every end-to-end
+    # repeat, never overwritten; results go to separate pinned buffers
+    host_in, host_out = [], []
     for lev in range(nlev):
         n = ctx.ncells(lev) * M.NQ
-        f = torch.empty(n, dtype=torch.float64, pin_memory=True)
-        g = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        f, g = pinned(n), pinned(n)
         ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
-        host.append((f, g))
+        host_in.append((f, g))
+        host_out.append((pinned(n), pinned(n)))
+
+    def download():
+        for lev, (f, g) in enumerate(host_out):
+            ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+
+    def upload():
+        for lev, (f, g) in enumerate(host_in):
+            ctx._check(lib.mbg_set_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
+
+    def finite():
+        return all(bool(torch.isfinite(f).all()) and bool(torch.isfinite(g).all()) for f, g in host_out)
+
     for _ in range(warmup):
         ctx.step(1)
     tuning = None
@@ -171,6 +209,8 @@ def run_form(form, steps, warmup, device_index):
         torch.cuda.nvtx.range_pop()
     ms = e0.elapsed_time(e1)
     launches = ctx.launch_count() - n0
+    download()
+    timed_finite = finite()
     # per-kernel device times: the same steps launched one by one between
     # CUDA events (the library's timing mode), for the roofline attribution
     ctx.set_timing(True)
@@ -186,13 +226,12 @@ def run_form(form, steps, warmup, device_index):
     # end to end through the C ABI with pinned host buffers: upload of the
     # initial state, K steps each followed by a read-back of its result (FP64:
     # the EB force, which the reference computes every step; 16-bit: the FP64
-    # conservation totals), download of the state.  One untimed round first:
-    # the first copies from freshly pinned buffers pay a one-time mapping cost
-    # (about 0.1 s on the GB300 machine), as the first steps pay for warm-up.  On
-    # the GB300 machine single state copies still stalled for 70-130 ms now and
-    # then within the first two rounds, so the whole timed sequence runs
-    # E2E_REPEATS times and the median wall time is reported, all of them
-    # listed beside it.
+    # conservation totals), download of the state.  Every repeat starts from
+    # the same host input.  One untimed round first: the first copies from
+    # freshly pinned buffers pay a one-time mapping cost, as the first steps
+    # pay for warm-up.  Single state copies have been seen to stall now and
+    # then, so the whole timed sequence runs E2E_REPEATS times and the median
+    # wall time is reported, all of them listed beside it.
     res_buf = torch.zeros(5, dtype=torch.float64, pin_memory=True)
     rb = C.cast(res_buf.data_ptr(), dp)
 
@@ -200,37 +239,33 @@ def run_form(form, steps, warmup, device_index):
         fn = lib.mbg_eb_forces if form == "fp64" else lib.mbg_conserved
         ctx._check(fn(ctx.h, rb), "result")
 
-    for lev, (f, g) in enumerate(host):
-        ctx._check(lib.mbg_set_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
-        ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+    upload()
+    download()
     result()
     ctx.synchronize()
-    walls, dev_ms = [], []
+    walls, dev_ms, rep_finite = [], [], []
     for _ in range(E2E_REPEATS):
         t0 = time.perf_counter()
         e0.record(stream)
-        for lev, (f, g) in enumerate(host):
-            ctx._check(lib.mbg_set_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "set")
+        upload()
         for _ in range(steps):
             ctx.step(1)
             result()
-        for lev, (f, g) in enumerate(host):
-            ctx._check(lib.mbg_get_state(ctx.h, lev, C.cast(f.data_ptr(), dp), C.cast(g.data_ptr(), dp)), "get")
+        download()
         e1.record(stream)
         e1.synchronize()
         walls.append(time.perf_counter() - t0)
         dev_ms.append(e0.elapsed_time(e1))
+        rep_finite.append(finite())
     k = sorted(range(len(walls)), key=lambda i: walls[i])[len(walls) // 2]
     wall = walls[k]
-    state_bytes = sum(2 * f.numel() * 8 for f, _ in host)
+    state_bytes = sum(2 * f.numel() * 8 for f, _ in host_in)
     res["e2e"] = {"value": cups * steps / wall / 1e6, "unit": "MLUPS",
                   "h2d_bytes_per_step": state_bytes / steps,
                   "d2h_bytes_per_step": state_bytes / steps + (24 if form == "fp64" else 40),
-                  "wall_s": wall, "device_ms": dev_ms[k], "repeats_wall_s": walls}
-    finite = True
-    for lev, (f, g) in enumerate(host):
-        finite &= bool(torch.isfinite(f).all()) and bool(torch.isfinite(g).all())
-    res["state_finite"] = finite
+                  "wall_s": wall, "device_ms": dev_ms[k], "repeats_wall_s": walls,
+                  "input": "the same initial state uploaded from pinned host memory in every repeat"}
+    res["state_finite"] = bool(timed_finite and all(rep_finite))
     d.close()
     return res
 
@@ -268,7 +303,10 @@ def run_batch(form, steps, warmup, device_index, count=256):
     import inputs
     import marbles_gb300 as M
 
-    doms = inputs.batch_domains(count)
+    # the literal nu ~ U[0.002, 0.02] at RT = 1/3 is unstable in the scheme
+    # (tests/test_stability.py); the same seeds drawn into U[0.15, 0.2] give the
+    # same cell counts and velocities at a stable viscosity
+    doms = inputs.batch_domains(count, nu_range=BATCH_NU)
     states = batch_states(doms)
     nv = sum(int(np.prod(n)) for n, _, _ in doms)
     f = torch.empty(nv * M.NQ, dtype=torch.float64, pin_memory=True)
@@ -282,8 +320,8 @@ def run_batch(form, steps, warmup, device_index, count=256):
     common.precision = PRECISION[form]
     common.rho_ref, common.t_ref = 1.0, 1.0 / 3.0
     out = {"workload": "batch of %d periodic Taylor-Green domains (cells per axis from {16, 24, ..., 96}, "
-                       "v0 ~ U[0.01, 0.08], nu ~ U[0.002, 0.02], seeds 0..%d), %.1f M cells"
-                       % (count, count - 1, nv / 1e6)}
+                       "v0 ~ U[0.01, 0.08], nu ~ U[%g, %g], seeds 0..%d), %.1f M cells"
+                       % (count, BATCH_NU[0], BATCH_NU[1], count - 1, nv / 1e6)}
     dp = C.POINTER(C.c_double)
     lib = M.lib()
     if form != "fp64":
@@ -398,54 +436,82 @@ def run_adjoint(steps, K, n=128, nu=0.01):
             "final_state_finite": bool(np.isfinite(Tf).all())}
 
 
-STEP_KERNEL = {"fp64": "k_collide", "fp16": "k_lowp_step", "bf16": "k_lowp_step"}
+# the level step's kernel class per form: the passes that read and write
+# every population (the FP64 form's two passes, the 16-bit step's launches)
+STEP_CLASS = {"fp64": ("k_moments", "k_collide"), "fp16": ("k_lowp_step",), "bf16": ("k_lowp_step",)}
 
 
-def roofline(res, form):
-    """Roofline of the level step's kernel class (the pass that reads and
-    writes every population: k_collide in FP64, the 16-bit step's launches),
-    whose algorithmic bytes are the per-cell figure; the coarse-fine
-    transfers are listed with their times in `kernels`."""
+def counters():
+    """Per-cell-update hardware counters of the step class, measured by ncu on
+    the 64^3 pulse (profiles/counters.json): DRAM bytes, and for the FP64 form
+    the FP64-pipe warp instructions with the pipe's peak issue rate."""
+    path = os.path.join(ROOT, "profiles", "counters.json")
+    return json.load(open(path)) if os.path.exists(path) else {}
+
+
+def roofline(res, form, sms):
+    """Roofline of the level step's kernel class.  HBM: algorithmic bytes
+    (865 B FP64, 217 B 16-bit per cell-update) over the class's summed event
+    time against the measured copy bandwidth.  FP64 form: also the FP64-pipe
+    bound -- the class's FP64 warp instructions per cell-update (ncu) against
+    the pipe's peak issue rate per SM and clock at the median SM clock sampled
+    during the timed steps; the lower of the two bounds is the roofline."""
     pk = peaks()
-    name = STEP_KERNEL[form]
-    kv = res["kernels"][name]
-    # algorithmic bytes per launch: per-cell figure x cells the launch updates
-    per_cell = BYTES_PER_CELL[form]
+    names = [n for n in STEP_CLASS[form] if n in res["kernels"]]
+    ms = sum(res["kernels"][n]["ms"] for n in names)
+    launches = sum(res["kernels"][n]["launches"] for n in names)
     cells = res["cell_updates_per_step"] * res["kernels_steps"]
-    if name == "k_moments":
-        per_cell = 432 + 1 if form == "fp64" else per_cell
-    achieved = per_cell * cells / (kv["ms"] * 1e-3) / 1e9
-    # DRAM bytes of one average launch of the class: the per-cell-update
-    # figure measured by ncu on the profiling case (profiles/traffic.json)
-    # times the cell-updates per launch here
+    per_cell = BYTES_PER_CELL[form]
+    t = ms * 1e-3
+    hbm_achieved = per_cell * cells / t / 1e9
+    cnt = counters().get(form, {})
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        t = json.load(open(tp)).get(form, {}).get(name)
-        if t and kv.get("launches"):
-            traffic = t["bytes_per_cell_update"] * cells / kv["launches"]
-    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if not pk.get("fallback") else "fallback",
-            "bytes_per_cell": per_cell}
+    if cnt.get("dram_bytes_per_cell_update") and launches:
+        traffic = cnt["dram_bytes_per_cell_update"] * cells / launches
+    hbm = {"bound": "hbm", "achieved": hbm_achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+           "frac": hbm_achieved / pk["hbm_gbs"],
+           "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if not pk.get("fallback") else "fallback",
+           "glups_bound": pk["hbm_gbs"] / per_cell}
+    out = dict(hbm)
+    out.update({"kernel": "+".join(names), "launches": launches, "traffic": traffic,
+                "traffic_unit": "DRAM bytes per launch (ncu, scaled by cell-updates)", "bytes_per_cell": per_cell})
+    if form == "fp64" and cnt.get("fp64_warp_inst_per_cell_update"):
+        clk = (res.get("clocks") or {}).get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+        x = cnt["fp64_warp_inst_per_cell_update"]
+        rate = sms * cnt["fp64_warp_inst_per_sm_per_cycle"] * clk * 1e6      # warp instructions / s
+        fp64 = {"bound": "fp64", "achieved": 32 * x * cells / t / 1e9, "peak": 32 * rate / 1e9,
+                "unit": "G FP64 thread-instructions/s", "frac": (x * cells / t) / rate,
+                "peak_source": "ncu sm__inst_executed_pipe_fp64.avg.peak_sustained x %d SMs x median SM clock "
+                               "%.0f MHz" % (sms, clk),
+                "glups_bound": rate / x / 1e9}
+        out["bounds"] = {"hbm": hbm, "fp64": fp64}
+        if fp64["glups_bound"] < hbm["glups_bound"]:
+            out.update({k: fp64[k] for k in ("bound", "achieved", "peak", "unit", "frac", "peak_source")})
+    return out
 
 
-def cpu_baseline(sample_steps=1):
-    """The FP64 oracle (port of the reference step) on the host cores, on a
-    bounded sample: initialisation excluded, sample_steps coarse steps."""
+def cpu_baseline(runs=3, sample_steps=10):
+    """The FP64 oracle (port of the reference step) on all host cores: the
+    median of `runs` timed runs of `sample_steps` coarse steps of the full
+    workload, initialisation excluded."""
     import cases
-    p, levels = cases.gaussian_pulse()
+    p, levels = cases.gaussian_pulse(t0=PULSE_T0)
     p.nthreads = os.cpu_count() or 1
     from oracle import oracle as O
     o = O.Oracle(p, levels)
     o.init()
-    t = time.perf_counter()
-    o.step(sample_steps)
-    dt = time.perf_counter() - t
+    times = []
+    for _ in range(runs):
+        t = time.perf_counter()
+        o.step(sample_steps)
+        times.append(time.perf_counter() - t)
+    dt = statistics.median(times)
     cups = sum(o.ncells(l) * 2 ** l for l in range(len(levels)))
+    o.close()
     return {"value": cups * sample_steps / dt / 1e6, "unit": "MLUPS", "cores": p.nthreads, "kind": "port",
-            "sample": "%d coarse step(s) of the full workload (%d cell-updates each), init excluded"
-                      % (sample_steps, cups)}
+            "sample": "median of %d runs of %d coarse steps of the full workload (%d cell-updates each), "
+                      "init excluded; oracle built -O3 -ffp-contract=off" % (runs, sample_steps, cups),
+            "runs_s": times}
 
 
 def dist_setup(n):
@@ -481,7 +547,7 @@ def main():
         # absent); its CPU path is timed through the oracle port
         import cases
         from oracle import oracle as O
-        p, levels = cases.gaussian_pulse()
+        p, levels = cases.gaussian_pulse(t0=PULSE_T0)
         p.nthreads = os.cpu_count() or 1
         o = O.Oracle(p, levels)
         o.init()
@@ -497,7 +563,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "form": "fp64 CPU", "parallelism": "host threads"},
             "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": p.nthreads, "kind": "port",
-                             "sample": "%d coarse steps of the full workload" % a.steps},
+                             "sample": "%d coarse steps of the full workload after %d warm-up steps"
+                                       % (a.steps, a.warmup)},
             "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
 
@@ -523,12 +590,16 @@ def main():
                 res[form] = {"error": str(ex)[:300]}
         if rank == 0:
             h = res.get("fp16", {})
+            bad = [f for f, r in res.items() if "state_finite" in r and not r["state_finite"]]
             print(json.dumps({"metric": "MLUPS", "value": h.get("mlups"), "unit": "MLUPS", "n_gpus": world,
                               "steps": a.steps, "warmup": a.warmup, "ms_per_step": h.get("ms_per_step"),
                               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                               "data": "synthetic", "config": {"workload": h.get("workload"), "form": "fp16"},
                               "e2e": h.get("e2e"), "gpu_launches": h.get("gpu_launches"),
                               "clocks": h.get("clocks"), "forms": res}))
+            if bad:
+                print("non-finite state in form(s): %s" % ", ".join(bad), file=sys.stderr)
+                sys.exit(1)
         return
     forms = ["fp64", "fp16", "bf16"] if a.form == "all" else a.form.split(",")
     results = {}
@@ -543,13 +614,13 @@ def main():
                 torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
                 r["ms_per_step"] = float(t.item())
                 r["mlups"] = r["cell_updates_per_step"] / (r["ms_per_step"] * 1e-3) / 1e6 * world
-            r["roofline"] = roofline(r, form)
+            r["roofline"] = roofline(r, form, torch.cuda.get_device_properties(dev).multi_processor_count)
             results[form] = r
         except Exception as ex:  # a form that is not built yet is reported, not fatal
             results[form] = {"error": str(ex)[:300]}
     if rank != 0:
         return
-    head = next((f for f in ("fp16", "bf16", "fp64") if f in results and "mlups" in results[f]), None)
+    head = next((f for f in ("fp64", "fp16", "bf16") if f in results and "mlups" in results[f]), None)
     if head is None:
         print(json.dumps({"metric": "MLUPS", "value": None, "error": results}))
         sys.exit(1)
@@ -558,9 +629,11 @@ def main():
         "metric": "MLUPS", "value": h["mlups"], "unit": "MLUPS", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": h["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD if a.workload == "pulse128" else a.workload, "form": head, "l2": "state larger than L2 (no flush needed)",
+        "config": {"workload": WORKLOAD if a.workload == "pulse128" else a.workload, "form": head,
+                   "l2": "state larger than L2 (no flush needed)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": h["roofline"], "e2e": h["e2e"], "gpu_launches": h["gpu_launches"], "clocks": h["clocks"],
+        "state_finite": h["state_finite"],
         "forms": {f: {k: v for k, v in r.items() if k not in ("kernels_steps",)} for f, r in results.items()},
     }
     if not a.no_cpu_baseline:
@@ -569,6 +642,10 @@ def main():
         except Exception as ex:
             line["cpu_baseline"] = {"error": str(ex)[:200]}
     print(json.dumps(line))
+    bad = [f for f, r in results.items() if not r.get("state_finite", False)]
+    if bad:
+        print("non-finite state (or failed run) in form(s): %s" % ", ".join(bad), file=sys.stderr)
+        sys.exit(1)
 
 
 if __name__ == "__main__":

@@ -149,9 +149,22 @@ mbg_status mbg_fillpatch(mbg_ctx* ctx, int lev);
 mbg_status mbg_average_down(mbg_ctx* ctx, int crse_lev, int crse_ng);
 
 /* Momentum-exchange force on embedded-boundary cells summed over all levels
- * (cells not covered by a finer level), FP64 accumulation.  Replaces
- * LBM::compute_eb_forces (Source/LBM.cpp:994-1044). */
+ * (cells not covered by a finer level), FP64 accumulation in a fixed order
+ * (per-block sums by warp shuffles, then one fixed-order sum of the blocks):
+ * the same state gives the same bits on every call.  16-bit forms: the
+ * stored populations decoded to FP64 (ghost fabs of fine levels excluded).
+ * Replaces LBM::compute_eb_forces (Source/LBM.cpp:994-1044). */
 mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3]);
+
+/* Derived fields of the stored state of level lev (7 components in the
+ * order of Source/Constants.H: vort_x, vort_y, vort_z, vort_mag, dQCorrX,
+ * dQCorrY, dQCorrZ), layout of mbg_get_macro: the vorticity and the
+ * q-correction gradients of the macro fields of the stored populations, by
+ * the reference's central / one-sided differences with the physical 1/dx,
+ * at fluid cells (0 elsewhere).  Replaces compute_derived and
+ * compute_q_corrections (Source/LBM.cpp:909-991) after f_to_macrodata, as
+ * the reference's output and restart paths call them. */
+mbg_status mbg_get_derived(mbg_ctx* ctx, int lev, double* derived);
 
 /* Conserved totals of the stored state over all levels, each cell counted on
  * the finest level that holds it and weighted by its volume, summed on the
@@ -279,6 +292,30 @@ void mbg_adj_destroy(mbg_adj* a);
 mbg_status mbg_step_box_noalloc(const mbg_params* params, const double* f_in, const double* g_in,
                                 double* f_out, double* g_out, void* cuda_stream);
 
+/* ---- AMReX-format files (host only, no device work) ------------------------
+ * Errors are reported by mbg_last_error(NULL).
+ *
+ * mbg_write_plotfile writes an AMReX plotfile directory (HyperCLaw-V1.1
+ * Header, Level_<l>/Cell_H and Cell_D_00000) of nlev levels at ratio 2:
+ * nbox[l] boxes per level, lohi the boxes of all levels concatenated (6 ints
+ * each, inclusive, in the level's index space), n_cell the level-0 domain,
+ * ncomp components named varnames, data[l] the level's values [box][comp]
+ * [k][j][i].  Replaces amrex::WriteMultiLevelPlotfile as LBM::write_plot_file
+ * calls it (Source/LBM.cpp:1677-1690). */
+mbg_status mbg_write_plotfile(const char* dir, int nlev, const int* nbox, const int* lohi, const int* n_cell,
+                              const double* prob_lo, const double* prob_hi, int ncomp,
+                              const char* const* varnames, const double* const* data, double time,
+                              const int* level_steps);
+
+/* A VisMF multifab <prefix>_H + <prefix>_D_00000 of nbox boxes (valid cells,
+ * no ghost cells), data [box][comp][k][j][i].  mbg_read_multifab reads one
+ * back into the same layout; the file's boxes must equal lohi (files with
+ * ghost cells are accepted, their valid region is kept).  Replace
+ * amrex::VisMF::Write / VisMF::Read of the checkpoint's f and g
+ * (Source/LBM.cpp:1770-1782, 1883-1893). */
+mbg_status mbg_write_multifab(const char* prefix, int nbox, const int* lohi, int ncomp, const double* data);
+mbg_status mbg_read_multifab(const char* prefix, int nbox, const int* lohi, int ncomp, double* data);
+
 /* ---- host drop-in driver ----------------------------------------------
  * The reference's LBM/AmrCore driver (Source/LBM.H:25-319, main.cpp:10-25)
  * on top of the entry points above: reads an inputs file with the
@@ -321,9 +358,23 @@ int mbg_lbm_num_levels(const mbg_lbm* h);
 mbg_status mbg_lbm_level_boxes(const mbg_lbm* h, int lev, int* lohi, int cap, int* nbox);
 mbg_status mbg_lbm_level_flags(const mbg_lbm* h, int lev, uint8_t* out, long long cap, long long* n);
 
-/* AMReX plotfile of the current state.  Replaces LBM::write_plot_file
- * (Source/LBM.cpp:1677-1690). */
+/* AMReX plotfile of the current state: the 19 macro fields of the stored
+ * populations, f and g (lbm.save_streaming), the 7 derived fields of
+ * mbg_get_derived (lbm.save_derived) and is_fluid / eb_boundary, with the
+ * reference's variable names.  Replaces LBM::write_plot_file
+ * (Source/LBM.cpp:1613-1690). */
 mbg_status mbg_lbm_write_plotfile(mbg_lbm* h, const char* name);
+
+/* Checkpoint directory of the current state: Header (title, finest level,
+ * steps, dts and times per level, box arrays) and Level_<l>/f_00, g_00
+ * multifabs.  A run whose inputs set amr.restart = <dir> resumes from it in
+ * mbg_lbm_init (the grids must be those the inputs build).  Replaces
+ * LBM::write_checkpoint_file / read_checkpoint_file
+ * (Source/LBM.cpp:1692-1916). */
+mbg_status mbg_lbm_write_checkpoint(mbg_lbm* h, const char* name);
+
+/* Coarse steps taken and the simulated time of the driver. */
+mbg_status mbg_lbm_step_time(const mbg_lbm* h, int* step, double* time);
 
 const char* mbg_lbm_last_error(const mbg_lbm* h);
 void mbg_lbm_destroy(mbg_lbm* h);

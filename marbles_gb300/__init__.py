@@ -26,7 +26,14 @@ EXPORTS = [
     "mbg_stream", "mbg_set_timing", "mbg_timing_count", "mbg_timing", "mbg_step_box_noalloc",
     "mbg_lbm_create", "mbg_lbm_prepare", "mbg_lbm_initial_state", "mbg_lbm_init", "mbg_lbm_evolve", "mbg_lbm_context", "mbg_lbm_num_levels",
     "mbg_lbm_level_boxes", "mbg_lbm_level_flags", "mbg_lbm_write_plotfile", "mbg_lbm_last_error",
-    "mbg_lbm_destroy",
+    "mbg_lbm_destroy", "mbg_lbm_write_checkpoint", "mbg_lbm_step_time",
+    "mbg_get_derived", "mbg_conserved", "mbg_autotune", "mbg_tuning",
+    "mbg_write_plotfile", "mbg_write_multifab", "mbg_read_multifab",
+    "mbg_batch_create", "mbg_batch_cells", "mbg_batch_set_state", "mbg_batch_get_state", "mbg_batch_get_macro",
+    "mbg_batch_step", "mbg_batch_autotune", "mbg_batch_tuning", "mbg_batch_synchronize", "mbg_batch_launch_count",
+    "mbg_batch_stream", "mbg_batch_last_error", "mbg_batch_destroy",
+    "mbg_adj_create", "mbg_adj_forward", "mbg_adj_backward", "mbg_adj_launch_count", "mbg_adj_stream",
+    "mbg_adj_last_error", "mbg_adj_destroy",
 ]
 
 
@@ -82,6 +89,13 @@ def lib():
         L.mbg_set_state.argtypes = [vp, C.c_int, dp, dp]
         L.mbg_get_state.argtypes = [vp, C.c_int, dp, dp]
         L.mbg_get_macro.argtypes = [vp, C.c_int, dp]
+        L.mbg_get_derived.argtypes = [vp, C.c_int, dp]
+        L.mbg_write_plotfile.argtypes = [C.c_char_p, C.c_int, ip, ip, ip, dp, dp, C.c_int,
+                                         C.POINTER(C.c_char_p), C.POINTER(dp), C.c_double, ip]
+        L.mbg_write_multifab.argtypes = [C.c_char_p, C.c_int, ip, C.c_int, dp]
+        L.mbg_read_multifab.argtypes = [C.c_char_p, C.c_int, ip, C.c_int, dp]
+        L.mbg_lbm_write_checkpoint.argtypes = [vp, C.c_char_p]
+        L.mbg_lbm_step_time.argtypes = [vp, ip, dp]
         L.mbg_step.argtypes = [vp, C.c_int]
         L.mbg_advance_level.argtypes = [vp, C.c_int]
         L.mbg_fillpatch.argtypes = [vp, C.c_int]
@@ -226,6 +240,12 @@ class Context:
     def get_macro(self, lev):
         m = np.empty(self.ncells(lev) * NMACRO)
         self._check(self.L.mbg_get_macro(self.h, lev, _dp(m)), "mbg_get_macro")
+        return m
+
+    def get_derived(self, lev):
+        """vort_x, vort_y, vort_z, vort_mag, dQCorrX..Z of the stored state, [box][7][cell]."""
+        m = np.empty(self.ncells(lev) * 7)
+        self._check(self.L.mbg_get_derived(self.h, lev, _dp(m)), "mbg_get_derived")
         return m
 
     def step(self, n=1):
@@ -508,6 +528,15 @@ class LBM:
     def write_plotfile(self, name):
         self._check(self.L.mbg_lbm_write_plotfile(self.h, name.encode()), "mbg_lbm_write_plotfile")
 
+    def write_checkpoint(self, name):
+        self._check(self.L.mbg_lbm_write_checkpoint(self.h, name.encode()), "mbg_lbm_write_checkpoint")
+
+    def step_time(self):
+        """(coarse steps taken, simulated time)"""
+        n, t = C.c_int(), C.c_double()
+        self._check(self.L.mbg_lbm_step_time(self.h, C.byref(n), C.byref(t)), "mbg_lbm_step_time")
+        return n.value, t.value
+
     def close(self):
         if getattr(self, "h", None):
             self.L.mbg_lbm_destroy(self.h)
@@ -518,3 +547,46 @@ class LBM:
             self.close()
         except Exception:
             pass
+
+
+def _io_check(st, what):
+    if st != 0:
+        raise MbgError("%s: %s: %s" % (what, STATUS.get(st, st), lib().mbg_last_error(None).decode()))
+
+
+def write_plotfile(path, levels, data, varnames, n_cell, prob_lo, prob_hi, time=0.0, level_steps=None):
+    """AMReX plotfile of host data (no GPU work): levels = [(nbox, 6) lo/hi],
+    data = [array [box][comp][cell] per level], varnames one per component."""
+    L = lib()
+    nlev = len(levels)
+    nbox = np.array([len(b) for b in levels], dtype=np.int32)
+    lohi = np.ascontiguousarray(np.concatenate([np.asarray(b, dtype=np.int32).reshape(-1) for b in levels]))
+    arrs = [np.ascontiguousarray(d, dtype=np.float64) for d in data]
+    ptrs = (C.POINTER(C.c_double) * nlev)(*[_dp(a) for a in arrs])
+    names = (C.c_char_p * len(varnames))(*[v.encode() for v in varnames])
+    steps = np.asarray(level_steps if level_steps is not None else [0] * nlev, dtype=np.int32)
+    nc = np.asarray(n_cell, dtype=np.int32)
+    lo = np.asarray(prob_lo, dtype=np.float64)
+    hi = np.asarray(prob_hi, dtype=np.float64)
+    ipt = C.POINTER(C.c_int)
+    _io_check(L.mbg_write_plotfile(path.encode(), nlev, nbox.ctypes.data_as(ipt), lohi.ctypes.data_as(ipt),
+                                   nc.ctypes.data_as(ipt), _dp(lo), _dp(hi), len(varnames), names, ptrs,
+                                   float(time), steps.ctypes.data_as(ipt)), "mbg_write_plotfile")
+
+
+def write_multifab(prefix, boxes, ncomp, data):
+    """VisMF multifab <prefix>_H / <prefix>_D_00000 of host data [box][comp][cell]."""
+    b = np.ascontiguousarray(np.asarray(boxes, dtype=np.int32).reshape(-1))
+    d = np.ascontiguousarray(data, dtype=np.float64)
+    _io_check(lib().mbg_write_multifab(prefix.encode(), len(b) // 6, b.ctypes.data_as(C.POINTER(C.c_int)), ncomp,
+                                       _dp(d)), "mbg_write_multifab")
+
+
+def read_multifab(prefix, boxes, ncomp):
+    b = np.ascontiguousarray(np.asarray(boxes, dtype=np.int32).reshape(-1))
+    bb = b.reshape(-1, 6)
+    n = int(np.prod(bb[:, 3:] - bb[:, :3] + 1, axis=1).sum())
+    out = np.empty(n * ncomp)
+    _io_check(lib().mbg_read_multifab(prefix.encode(), len(bb), b.ctypes.data_as(C.POINTER(C.c_int)), ncomp,
+                                      _dp(out)), "mbg_read_multifab")
+    return out

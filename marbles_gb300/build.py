@@ -30,6 +30,7 @@ UNITS = {
     "mbg_capi.cu": [],
     "lbm_driver.cu": [],
     "lbm_capi.cu": [],
+    "lbm_io.cu": [],
     "mbg_noalloc.cu": ["-fmad=false"],
 }
 EXE = os.path.join(HERE, "marbles_gb300_run")
@@ -41,9 +42,18 @@ def nvcc():
             return c
 
 
+def _headers_mtime():
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    hs.append(os.path.join(HERE, "..", "include", "marbles_gb300.h"))
+    return max(os.path.getmtime(h) for h in hs if os.path.exists(h))
+
+
 def _compile(unit, extra):
     src = os.path.join(CSRC, unit)
     obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
+    # an object newer than its source and every header is kept
+    if os.path.exists(obj) and os.path.getmtime(obj) > max(os.path.getmtime(src), _headers_mtime()):
+        return obj
     cmd = [nvcc()] + COMMON + extra + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -112,6 +112,22 @@ mbg_status mbg_lbm_write_plotfile(mbg_lbm* h, const char* name)
     return st;
 }
 
+mbg_status mbg_lbm_write_checkpoint(mbg_lbm* h, const char* name)
+{
+    if (!h || !name) return MBG_EINVAL;
+    mbg_status st = h->lbm.write_checkpoint(name);
+    if (st != MBG_OK) h->err = h->lbm.err;
+    return st;
+}
+
+mbg_status mbg_lbm_step_time(const mbg_lbm* h, int* step, double* time)
+{
+    if (!h) return MBG_EINVAL;
+    if (step) *step = h->lbm.step();
+    if (time) *time = h->lbm.time();
+    return MBG_OK;
+}
+
 const char* mbg_lbm_last_error(const mbg_lbm* h) { return h ? h->err.c_str() : g_lbm_err.c_str(); }
 
 void mbg_lbm_destroy(mbg_lbm* h) { delete h; }

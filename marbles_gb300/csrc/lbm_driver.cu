@@ -2,6 +2,7 @@
 // only; compiled by nvcc so that it shares mbg_physics.cuh with the
 // kernels).  See lbm_driver.h.
 #include <algorithm>
+#include <cerrno>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -220,6 +221,7 @@ bool LBM::configure(const Inputs& in, std::string& e)
     in.query("amr.chk_int", c.chk_int);
     in.query("amr.chk_file", c.chk_file);
     in.query("amr.file_name_digits", c.file_name_digits);
+    in.query("amr.restart", c.restart);
     std::vector<double> dv;
     if (!need3(in, "geometry.prob_lo", dv, e)) return false;
     for (int d = 0; d < 3; ++d) c.prob_lo[d] = dv[d];
@@ -794,25 +796,43 @@ mbg_status LBM::init_data()
             for (int x : {b.lo[0], b.lo[1], b.lo[2], b.hi[0], b.hi[1], b.hi[2]}) lohi.push_back(x);
         st = mbg_define_level(ctx_, (int)lev, (int)grids_[lev].size(), lohi.data(), flags_[lev].data());
         if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
+        if (!cfg_.restart.empty()) continue;
         std::vector<double> f, g;
         initial_state((int)lev, f, g);
         st = mbg_set_state(ctx_, (int)lev, f.data(), g.data());
         if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
     }
-    for (int lev = (int)grids_.size() - 2; lev >= 0; --lev) {
-        st = mbg_average_down(ctx_, lev, 0);
-        if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
+    if (!cfg_.restart.empty()) {
+        // LBM::init_data's restart branch (Source/LBM.cpp:177-182)
+        st = read_checkpoint();
+        if (st != MBG_OK) return st;
+        if (cfg_.compute_forces) write_forces(false);
+    } else {
+        for (int lev = (int)grids_.size() - 2; lev >= 0; --lev) {
+            st = mbg_average_down(ctx_, lev, 0);
+            if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
+        }
+        step_ = 0;
+        time_ = 0.0;
+        if (cfg_.chk_int > 0) {
+            st = write_checkpoint(numbered(cfg_.chk_file));
+            if (st != MBG_OK) return st;
+        }
+        if (cfg_.compute_forces) write_forces(true);
     }
-    step_ = 0;
-    time_ = 0.0;
-    if (cfg_.compute_forces) write_forces(true);
     if (cfg_.plot_int > 0) {
-        char name[64];
-        std::snprintf(name, sizeof name, "%s%0*d", cfg_.plot_file.c_str(), cfg_.file_name_digits, step_);
-        st = write_plot_file(name);
+        st = write_plot_file(numbered(cfg_.plot_file));
         if (st != MBG_OK) return st;
     }
     return MBG_OK;
+}
+
+// amrex::Concatenate(root, step, file_name_digits)
+std::string LBM::numbered(const std::string& root) const
+{
+    char num[32];
+    std::snprintf(num, sizeof num, "%0*d", cfg_.file_name_digits, step_);
+    return root + num;
 }
 
 void LBM::write_forces(bool init)
@@ -825,7 +845,10 @@ void LBM::write_forces(bool init)
 
 mbg_status LBM::evolve(int nsteps)
 {
-    const int last = nsteps > 0 ? step_ + nsteps : cfg_.max_step;
+    // LBM::evolve (Source/LBM.cpp:398-448): nsteps <= 0 runs to max_step /
+    // stop_time and then writes the last plotfile if it is not written yet
+    const bool to_end = nsteps <= 0;
+    const int last = to_end ? cfg_.max_step : step_ + nsteps;
     while (step_ < last && time_ < cfg_.stop_time) {
         mbg_status st = mbg_step(ctx_, 1);
         if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
@@ -833,18 +856,268 @@ mbg_status LBM::evolve(int nsteps)
         time_ += 1.0;
         if (cfg_.compute_forces) write_forces(false);
         if (cfg_.plot_int > 0 && step_ % cfg_.plot_int == 0) {
-            char name[64];
-            std::snprintf(name, sizeof name, "%s%0*d", cfg_.plot_file.c_str(), cfg_.file_name_digits, step_);
-            st = write_plot_file(name);
+            st = write_plot_file(numbered(cfg_.plot_file));
             if (st != MBG_OK) return st;
         }
+        if (cfg_.chk_int > 0 && step_ % cfg_.chk_int == 0) {
+            st = write_checkpoint(numbered(cfg_.chk_file));
+            if (st != MBG_OK) return st;
+        }
+    }
+    if (to_end && cfg_.plot_int > 0 && step_ > last_plot_step_) {
+        mbg_status st = write_plot_file(numbered(cfg_.plot_file));
+        if (st != MBG_OK) return st;
     }
     return mbg_synchronize(ctx_);
 }
 
-mbg_status LBM::write_plot_file(const std::string&)
+// ---------------------------------------------------------------------------
+// plotfile and checkpoint (Source/LBM.cpp:1613-1916)
+// ---------------------------------------------------------------------------
+namespace {
+
+const char* const MACRO_NAMES[19] = {"rho", "vel_x", "vel_y", "vel_z", "vel_mag", "two_rho_e", "QCorrX",
+                                     "QCorrY", "QCorrZ", "pxx", "pyy", "pzz", "pxy", "pxz", "pyz",
+                                     "qx", "qy", "qz", "temperature"};
+const char* const DERIVED_NAMES[7] = {"vort_x", "vort_y", "vort_z", "vort_mag", "dQCorrX", "dQCorrY", "dQCorrZ"};
+
+std::string two_digits(const char* pre, int q)
 {
-    return MBG_OK;  // plotfile writer: see lbm_plotfile.cu
+    char b[16];
+    std::snprintf(b, sizeof b, "%s%02d", pre, q);
+    return b;
+}
+
+bool mkdir_p(const std::string& d)
+{
+    if (mkdir(d.c_str(), 0755) == 0) return true;
+    struct stat st;
+    return errno == EEXIST && stat(d.c_str(), &st) == 0 && S_ISDIR(st.st_mode);
+}
+
+std::vector<int> lohi_of(const std::vector<Box>& ba)
+{
+    std::vector<int> v;
+    for (const Box& b : ba)
+        for (int x : {b.lo[0], b.lo[1], b.lo[2], b.hi[0], b.hi[1], b.hi[2]}) v.push_back(x);
+    return v;
+}
+
+}  // namespace
+
+mbg_status LBM::write_plot_file(const std::string& name)
+{
+    if (!ctx_) { err = "write_plot_file: the driver is not initialised"; return MBG_ESTATE; }
+    // variable list of LBM::LBM (Source/LBM.cpp:14-82): macro, f, g, derived, flags
+    std::vector<std::string> names(MACRO_NAMES, MACRO_NAMES + 19);
+    if (cfg_.save_streaming) {
+        for (int q = 0; q < mbg::NQ; ++q) names.push_back(two_digits("f_", q));
+        for (int q = 0; q < mbg::NQ; ++q) names.push_back(two_digits("g_", q));
+    }
+    if (cfg_.save_derived) names.insert(names.end(), DERIVED_NAMES, DERIVED_NAMES + 7);
+    names.push_back("is_fluid");
+    names.push_back("eb_boundary");
+    const int nc = (int)names.size();
+    const int nlev = (int)grids_.size();
+    std::vector<std::vector<double>> data(nlev);
+    std::vector<const double*> ptrs(nlev);
+    std::vector<int> nbox(nlev), steps(nlev), lohi;
+    for (int lev = 0; lev < nlev; ++lev) {
+        const std::vector<Box>& ba = grids_[lev];
+        long long ncell = 0;
+        for (const Box& b : ba) ncell += b.vol();
+        std::vector<double> mac((size_t)ncell * 19), f, g, der;
+        mbg_status st = mbg_get_macro(ctx_, lev, mac.data());
+        if (st == MBG_OK && cfg_.save_streaming) {
+            f.resize((size_t)ncell * mbg::NQ);
+            g.resize((size_t)ncell * mbg::NQ);
+            st = mbg_get_state(ctx_, lev, f.data(), g.data());
+        }
+        if (st == MBG_OK && cfg_.save_derived) {
+            der.resize((size_t)ncell * 7);
+            st = mbg_get_derived(ctx_, lev, der.data());
+        }
+        if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
+        std::vector<double>& D = data[lev];
+        D.resize((size_t)ncell * nc);
+        long long off = 0, foff = 0;
+        for (const Box& b : ba) {
+            const long long v = b.vol();
+            double* dst = D.data() + off * nc;
+            int c = 0;
+            auto put = [&](const double* src, int n) {
+                std::memcpy(dst + (size_t)c * v, src, (size_t)n * v * sizeof(double));
+                c += n;
+            };
+            put(mac.data() + off * 19, 19);
+            if (cfg_.save_streaming) {
+                put(f.data() + off * mbg::NQ, mbg::NQ);
+                put(g.data() + off * mbg::NQ, mbg::NQ);
+            }
+            if (cfg_.save_derived) put(der.data() + off * 7, 7);
+            // is_fluid components 0 and 1 of the valid cells
+            long long cell = 0;
+            for (int k = 0; k < b.n(2); ++k)
+                for (int j = 0; j < b.n(1); ++j)
+                    for (int i = 0; i < b.n(0); ++i, ++cell) {
+                        const uint8_t fl = flags_[lev][foff + ((long long)(k + 3) * (b.n(1) + 6) + (j + 3)) *
+                                                                  (b.n(0) + 6) + (i + 3)];
+                        dst[(size_t)c * v + cell] = (fl & 1) ? 1.0 : 0.0;
+                        dst[(size_t)(c + 1) * v + cell] = (fl & 2) ? 1.0 : 0.0;
+                    }
+            off += v;
+            foff += (long long)(b.n(0) + 6) * (b.n(1) + 6) * (b.n(2) + 6);
+        }
+        ptrs[lev] = D.data();
+        nbox[lev] = (int)ba.size();
+        steps[lev] = step_ << lev;
+        std::vector<int> l = lohi_of(ba);
+        lohi.insert(lohi.end(), l.begin(), l.end());
+    }
+    std::vector<const char*> cn;
+    for (const std::string& n : names) cn.push_back(n.c_str());
+    mbg_status st = mbg_write_plotfile(name.c_str(), nlev, nbox.data(), lohi.data(), cfg_.n_cell, cfg_.prob_lo,
+                                       cfg_.prob_hi, nc, cn.data(), ptrs.data(), time_, steps.data());
+    if (st != MBG_OK) { err = mbg_last_error(nullptr); return st; }
+    last_plot_step_ = step_;
+    return MBG_OK;
+}
+
+// LBM::write_checkpoint_file (Source/LBM.cpp:1692-1783): Header, then f and
+// g of every level as VisMF multifabs Level_<l>/f_00 and Level_<l>/g_00
+mbg_status LBM::write_checkpoint(const std::string& name)
+{
+    if (!ctx_) { err = "write_checkpoint: the driver is not initialised"; return MBG_ESTATE; }
+    const int nlev = (int)grids_.size();
+    if (!mkdir_p(name)) { err = "write_checkpoint: cannot create directory " + name; return MBG_EINVAL; }
+    {
+        std::ofstream h(name + "/Header", std::ios::trunc);
+        if (!h) { err = "write_checkpoint: cannot open " + name + "/Header"; return MBG_EINVAL; }
+        h.precision(17);
+        h << "Checkpoint file for LBM\n" << nlev - 1 << "\n";
+        for (int l = 0; l < nlev; ++l) h << (step_ << l) << " ";
+        h << "\n";
+        for (int l = 0; l < nlev; ++l) h << 1.0 / (double)(1 << l) << " ";
+        h << "\n";
+        for (int l = 0; l < nlev; ++l) h << time_ << " ";
+        h << "\n";
+        for (int l = 0; l < nlev; ++l) {
+            const std::vector<Box>& ba = grids_[l];
+            h << "(" << ba.size() << " 0\n";
+            for (const Box& b : ba)
+                h << "((" << b.lo[0] << "," << b.lo[1] << "," << b.lo[2] << ") (" << b.hi[0] << "," << b.hi[1] << ","
+                  << b.hi[2] << ") (0,0,0))\n";
+            h << ")\n";
+        }
+        h.close();
+        if (!h) { err = "write_checkpoint: write failed: " + name + "/Header"; return MBG_EINVAL; }
+    }
+    for (int lev = 0; lev < nlev; ++lev) {
+        const std::string ld = name + "/Level_" + std::to_string(lev);
+        if (!mkdir_p(ld)) { err = "write_checkpoint: cannot create directory " + ld; return MBG_EINVAL; }
+        long long ncell = 0;
+        for (const Box& b : grids_[lev]) ncell += b.vol();
+        std::vector<double> f((size_t)ncell * mbg::NQ), g((size_t)ncell * mbg::NQ);
+        mbg_status st = mbg_get_state(ctx_, lev, f.data(), g.data());
+        if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
+        const std::vector<int> lohi = lohi_of(grids_[lev]);
+        const int nb = (int)grids_[lev].size();
+        st = mbg_write_multifab((ld + "/f_00").c_str(), nb, lohi.data(), mbg::NQ, f.data());
+        if (st == MBG_OK) st = mbg_write_multifab((ld + "/g_00").c_str(), nb, lohi.data(), mbg::NQ, g.data());
+        if (st != MBG_OK) { err = mbg_last_error(nullptr); return st; }
+    }
+    return MBG_OK;
+}
+
+// LBM::read_checkpoint_file (Source/LBM.cpp:1785-1916) onto the static
+// grids the inputs build: the Header's box arrays must be those grids
+mbg_status LBM::read_checkpoint()
+{
+    const std::string& dir = cfg_.restart;
+    std::ifstream in(dir + "/Header");
+    if (!in) { err = "amr.restart: cannot read " + dir + "/Header"; return MBG_EINVAL; }
+    std::string line;
+    std::getline(in, line);
+    int finest = -1;
+    in >> finest;
+    std::getline(in, line);
+    const int nlev = (int)grids_.size();
+    if (finest != nlev - 1) {
+        err = "amr.restart: the checkpoint has " + std::to_string(finest + 1) + " levels, the inputs build " +
+              std::to_string(nlev);
+        return MBG_EINVAL;
+    }
+    std::vector<std::vector<double>> rows(3);
+    for (int r = 0; r < 3; ++r) {
+        std::getline(in, line);
+        std::istringstream ls(line);
+        double v;
+        while (ls >> v) rows[r].push_back(v);
+        if ((int)rows[r].size() != nlev) { err = "amr.restart: malformed Header in " + dir; return MBG_EINVAL; }
+    }
+    for (int l = 0; l < nlev; ++l) {
+        int n = -1, hash = 0;
+        char c = 0;
+        in >> c >> n >> hash;
+        if (c != '(' || n != (int)grids_[l].size()) {
+            err = "amr.restart: level " + std::to_string(l) + " of the checkpoint has other grids than the inputs "
+                  "build (run-time regridding is not supported)";
+            return MBG_EINVAL;
+        }
+        std::getline(in, line);
+        for (int b = 0; b < n; ++b) {
+            std::getline(in, line);
+            int v[9];
+            if (std::sscanf(line.c_str(), " ((%d,%d,%d) (%d,%d,%d) (%d,%d,%d))", &v[0], &v[1], &v[2], &v[3], &v[4],
+                            &v[5], &v[6], &v[7], &v[8]) != 9) {
+                err = "amr.restart: malformed box in " + dir + "/Header";
+                return MBG_EINVAL;
+            }
+            const Box& B = grids_[l][b];
+            if (v[0] != B.lo[0] || v[1] != B.lo[1] || v[2] != B.lo[2] || v[3] != B.hi[0] || v[4] != B.hi[1] ||
+                v[5] != B.hi[2]) {
+                err = "amr.restart: level " + std::to_string(l) + " box " + std::to_string(b) +
+                      " of the checkpoint differs from the grids the inputs build";
+                return MBG_EINVAL;
+            }
+        }
+        std::getline(in, line);   // ")"
+    }
+    for (int lev = 0; lev < nlev; ++lev) {
+        const std::string ld = dir + "/Level_" + std::to_string(lev);
+        long long ncell = 0;
+        for (const Box& b : grids_[lev]) ncell += b.vol();
+        std::vector<double> f((size_t)ncell * mbg::NQ), g((size_t)ncell * mbg::NQ);
+        const std::vector<int> lohi = lohi_of(grids_[lev]);
+        const int nb = (int)grids_[lev].size();
+        mbg_status st = mbg_read_multifab((ld + "/f_00").c_str(), nb, lohi.data(), mbg::NQ, f.data());
+        if (st == MBG_OK) st = mbg_read_multifab((ld + "/g_00").c_str(), nb, lohi.data(), mbg::NQ, g.data());
+        if (st != MBG_OK) { err = mbg_last_error(nullptr); return st; }
+        // fill_f_inside_eb (Source/LBM.cpp:1278-1298): solid cells start at 0
+        long long off = 0, foff = 0;
+        for (const Box& b : grids_[lev]) {
+            const long long v = b.vol();
+            long long cell = 0;
+            for (int k = 0; k < b.n(2); ++k)
+                for (int j = 0; j < b.n(1); ++j)
+                    for (int i = 0; i < b.n(0); ++i, ++cell) {
+                        const uint8_t fl = flags_[lev][foff + ((long long)(k + 3) * (b.n(1) + 6) + (j + 3)) *
+                                                                  (b.n(0) + 6) + (i + 3)];
+                        if (fl & 1) continue;
+                        for (int q = 0; q < mbg::NQ; ++q) {
+                            f[(size_t)(off * mbg::NQ + q * v + cell)] = 0.0;
+                            g[(size_t)(off * mbg::NQ + q * v + cell)] = 0.0;
+                        }
+                    }
+            off += v;
+            foff += (long long)(b.n(0) + 6) * (b.n(1) + 6) * (b.n(2) + 6);
+        }
+        st = mbg_set_state(ctx_, lev, f.data(), g.data());
+        if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
+    }
+    step_ = (int)rows[0][0];
+    time_ = rows[2][0];
+    return MBG_OK;
 }
 
 }  // namespace mbgdrv

@@ -57,6 +57,7 @@ struct Config {
     int regrid_int = 2;
     int plot_int = -1, chk_int = -1;
     std::string plot_file = "plt", chk_file = "chk";
+    std::string restart;   // amr.restart: checkpoint directory to resume from
     int file_name_digits = 5;
     // geometry.*
     double prob_lo[3] = {0, 0, 0}, prob_hi[3] = {1, 1, 1};
@@ -119,6 +120,7 @@ public:
     mbg_status init_data();
     mbg_status evolve(int nsteps);      // nsteps <= 0: run to max_step / stop_time
     mbg_status write_plot_file(const std::string& name);
+    mbg_status write_checkpoint(const std::string& name);
     mbg_ctx* context() { return ctx_; }
     const Config& config() const { return cfg_; }
     const std::vector<std::vector<Box>>& grids() const { return grids_; }
@@ -140,7 +142,11 @@ private:
     std::vector<std::vector<uint8_t>> flags_;
     int step_ = 0;
     double time_ = 0.0;
+    int last_plot_step_ = -1;
     bool prepared_ = false;
+
+    mbg_status read_checkpoint();
+    std::string numbered(const std::string& root) const;
 
     void level_geometry(int lev, double dx[3]) const;
     bool covered_cell(int lev, int i, int j, int k) const;

@@ -102,6 +102,12 @@ struct mbg_ctx {
     double* d_red = nullptr;   // small reduction scratch
     double* d_out19 = nullptr;
     size_t out19_n = 0;
+    // per-block partial sums of the EB force (3 per tile of every level)
+    double* d_partial = nullptr;
+    size_t partial_n = 0;
+    // FP64 decode of a 16-bit level's f and g for the output kernels
+    double* d_dec[2] = {nullptr, nullptr};
+    size_t dec_n[2] = {0, 0};
     std::vector<void*> allocs;
 };
 
@@ -281,8 +287,15 @@ mbg_status mbg_create(const mbg_params* params, void* cuda_stream, mbg_ctx** out
                 g_create_err = "mbg_create: BC is interior in direction " + std::to_string(d) + " but not periodic";
                 return MBG_EINVAL;
             }
-            if (c == 3) {
-                g_create_err = "mbg_create: the pressure boundary condition (code 3) is not supported";
+            if (c == 3 && !(p.is_periodic[(d + 1) % 3] && p.is_periodic[(d + 2) % 3])) {
+                // The reference's functor reads, for a pressure ghost cell, the
+                // populations around the adjacent interior cell; next to a
+                // non-periodic tangential side some of those are ghost cells that
+                // the same functor pass rewrites, so the result depends on the
+                // order the functor visits ghost cells.  With periodic
+                // tangential sides every read is a valid cell or a periodic copy.
+                g_create_err = "mbg_create: the pressure boundary condition (code 3) in direction " +
+                               std::to_string(d) + " needs periodic tangential directions";
                 return MBG_EINVAL;
             }
         }
@@ -968,17 +981,83 @@ mbg_status mbg_average_down(mbg_ctx* ctx, int crse_lev, int crse_ng)
     return MBG_OK;
 }
 
+// FP64 views of a level's stored populations for the output kernels: the
+// FP64 form's own buffers; the 16-bit forms' populations decoded into FP64
+// scratch of the context (f, and g when want_g), without their ghost fabs
+static mbg_status fp64_state(mbg_ctx* ctx, Level& L, bool want_g, const double** f, const double** g,
+                             const double** fg, const double** gg)
+{
+    if (ctx->p.precision == MBG_FP64) {
+        *f = L.f[L.cur];
+        *g = L.g[L.cur];
+        *fg = L.fg[L.cur];
+        *gg = L.gg[L.cur];
+        return MBG_OK;
+    }
+    const size_t need = (size_t)L.N * NQ;
+    for (int lat = 0; lat < (want_g ? 2 : 1); ++lat) {
+        if (ctx->dec_n[lat] < need) {
+            mbg_status st = dalloc(ctx, &ctx->d_dec[lat], need);
+            if (st != MBG_OK) return st;
+            ctx->dec_n[lat] = need;
+        }
+        lowp_decode(L.lowp, L.plan, lat, ctx->d_dec[lat], ctx->s);
+        ctx->launches++;
+    }
+    *f = ctx->d_dec[0];
+    *g = want_g ? ctx->d_dec[1] : nullptr;
+    *fg = nullptr;
+    *gg = nullptr;
+    return MBG_OK;
+}
+
 mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3])
 {
     if (!ctx || !out) return MBG_EINVAL;
-    if (ctx->p.precision != MBG_FP64) return fail(ctx, MBG_EINVAL, "mbg_eb_forces: FP64 form only");
-    MBG_CUDA(cudaMemsetAsync(ctx->d_red, 0, 3 * sizeof(double), ctx->s));
-    for (auto& L : ctx->lv) {
-        launch_eb_forces(L.plan, L.f[L.cur], L.fg[L.cur], ctx->d_red, ctx->s);
-        ctx->launches++;
+    if (ctx->lv.empty()) return fail(ctx, MBG_ESTATE, "mbg_eb_forces: no level defined");
+    long long nt = 0;
+    for (auto& L : ctx->lv) nt += L.ntiles;
+    if (ctx->partial_n < (size_t)nt * 3) {
+        mbg_status st = dalloc(ctx, &ctx->d_partial, (size_t)nt * 3);
+        if (st != MBG_OK) return st;
+        ctx->partial_n = (size_t)nt * 3;
     }
+    long long off = 0;
+    for (auto& L : ctx->lv) {
+        const double *f, *g, *fg, *gg;
+        mbg_status st = fp64_state(ctx, L, false, &f, &g, &fg, &gg);
+        if (st != MBG_OK) return st;
+        launch_eb_forces(L.plan, f, fg, ctx->d_partial + off * 3, ctx->s);
+        ctx->launches++;
+        off += L.ntiles;
+    }
+    launch_sum_partials(ctx->d_partial, nt, ctx->d_red, ctx->s);
+    ctx->launches++;
     MBG_CUDA(cudaGetLastError());
     MBG_CUDA(cudaMemcpyAsync(out, ctx->d_red, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+mbg_status mbg_get_derived(mbg_ctx* ctx, int lev, double* derived)
+{
+    if (!ctx || !derived) return MBG_EINVAL;
+    if (lev < 0 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_get_derived: level not defined");
+    Level& L = ctx->lv[lev];
+    const size_t need = (size_t)L.N * 19;
+    if (ctx->out19_n < need) {
+        mbg_status st = dalloc(ctx, &ctx->d_out19, need);
+        if (st != MBG_OK) return st;
+        ctx->out19_n = need;
+    }
+    const double *f, *g, *fg, *gg;
+    mbg_status st = fp64_state(ctx, L, true, &f, &g, &fg, &gg);
+    if (st != MBG_OK) return st;
+    launch_derived(L.plan, phys64(ctx, L), f, g, fg, gg, ctx->d_out19, ctx->s);
+    ctx->launches++;
+    MBG_CUDA(cudaGetLastError());
+    MBG_CUDA(cudaMemcpyAsync(derived, ctx->d_out19, (size_t)L.N * 7 * sizeof(double), cudaMemcpyDeviceToHost,
+                             ctx->s));
     MBG_CUDA(cudaStreamSynchronize(ctx->s));
     return MBG_OK;
 }

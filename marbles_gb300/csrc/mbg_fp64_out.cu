@@ -33,11 +33,115 @@ __global__ void k_macro_local(LV L, Phys64 ph, const Tile* tiles, const double* 
     for (int k = 0; k < 19; ++k) o[k * vol] = vals[k];
 }
 
-// ---- EB momentum-exchange force (Source/LBM.cpp:994-1044) -------------------
-// per-cell sums in FP64; only eb_boundary cells contribute (a thin shell), so
-// each such cell adds its three components with FP64 atomics
-__global__ void k_eb_forces(LV L, const Tile* tiles, const double* f, const double* fg, double* out3)
+// ---- derived fields of the current state (Source/LBM.cpp:909-991) ------------
+// macro fields of the stored populations of box-local cell (x, y, z): its own
+// valid cell, the owning box's (periodic images included) or, in the
+// coarse-fine shell, the box's ghost fab -- what f_to_macrodata computes over
+// the box grown by one (Source/LBM.cpp:810-906)
+__device__ __forceinline__ Macro<double> stored_macro(const LV& L, const Phys64& ph, const DevBox& B, int x, int y,
+                                                      int z, const double* f, const double* g, const double* fg,
+                                                      const double* gg)
 {
+    MomentAcc<double> acc;
+#define MBG_SM64(q) acc.template add<q>(fab_value(L, B, x, y, z, q, f, fg), fab_value(L, B, x, y, z, q, g, gg));
+    MBG_UNROLL27(MBG_SM64)
+#undef MBG_SM64
+    return acc.finish(ph.mesh_speed, ph.Rg, ph.cv);
+}
+
+__device__ __forceinline__ double macro_comp(const Macro<double>& m, int c)
+{
+    switch (c) {
+    case MD_U: return m.u;
+    case MD_V: return m.v;
+    case MD_W: return m.w;
+    case MD_QCX: return m.qcx;
+    case MD_QCY: return m.qcy;
+    case MD_QCZ: return m.qcz;
+    default: return m.rho;
+    }
+}
+
+// gradient() of Source/Utilities.H:279-312 along axis d of the macro
+// components comps[0..n) at once: central in the interior, one-sided where a
+// neighbour lies outside the domain box or is not fluid, 0 if both do
+template <int NC>
+__device__ __forceinline__ void grad_stored(const LV& L, const Phys64& ph, const DevBox& B, int x, int y, int z,
+                                            int d, const Macro<double>& mc, const double* f, const double* g,
+                                            const double* fg, const double* gg, const int (&comps)[NC],
+                                            double (&out)[NC])
+{
+    int pp[3] = {x, y, z}, pm[3] = {x, y, z};
+    pp[d] += 1;
+    pm[d] -= 1;
+    const bool p_out = B.lo[d] + pp[d] > L.dhi[d] || !(flag_at(L, B, pp[0], pp[1], pp[2]) & FL_FLUID);
+    const bool m_out = B.lo[d] + pm[d] < L.dlo[d] || !(flag_at(L, B, pm[0], pm[1], pm[2]) & FL_FLUID);
+    Macro<double> mp = mc, mm = mc;
+    if (!p_out) mp = stored_macro(L, ph, B, pp[0], pp[1], pp[2], f, g, fg, gg);
+    if (!m_out) mm = stored_macro(L, ph, B, pm[0], pm[1], pm[2], f, g, fg, gg);
+    for (int k = 0; k < NC; ++k) {
+        const double a = macro_comp(mp, comps[k]), c = macro_comp(mc, comps[k]), m = macro_comp(mm, comps[k]);
+        double vp = 0.0, vc = 0.0, vm = 0.0;
+        if (p_out && m_out) {
+            vp = 0.0; vc = 0.0; vm = 0.0;
+        } else if (p_out) {
+            vp = 0.0; vc = c; vm = -m;
+        } else if (m_out) {
+            vp = a; vc = -c; vm = 0.0;
+        } else {
+            vp = 0.5 * a; vc = 0.0; vm = -0.5 * m;
+        }
+        out[k] = (vp + vc + vm) * ph.idx[d];
+    }
+}
+
+// vort_x, vort_y, vort_z, vort_mag, dQCorrX, dQCorrY, dQCorrZ per fluid cell
+// (0 elsewhere), host layout [box][7][cell]
+__global__ void k_derived(LV L, Phys64 ph, const Tile* tiles, const double* f, const double* g, const double* fg,
+                          const double* gg, double* out7)
+{
+    int b, x, y, z;
+    long long c;
+    if (!cell_of_tile(L, tiles, b, x, y, z, c)) return;
+    const DevBox& B = L.box[b];
+    const long long vol = (long long)B.n[0] * B.n[1] * B.n[2];
+    double* o = out7 + B.hoff * 7 + c;
+    if (!(flag_at(L, B, x, y, z) & FL_FLUID)) {
+        for (int k = 0; k < 7; ++k) o[k * vol] = 0.0;
+        return;
+    }
+    const Macro<double> mc = stored_macro(L, ph, B, x, y, z, f, g, fg, gg);
+    double gx[3], gy[3], gz[3];
+    grad_stored(L, ph, B, x, y, z, 0, mc, f, g, fg, gg, {MD_V, MD_W, MD_QCX}, gx);   // vx, wx, dQx
+    grad_stored(L, ph, B, x, y, z, 1, mc, f, g, fg, gg, {MD_U, MD_W, MD_QCY}, gy);   // uy, wy, dQy
+    grad_stored(L, ph, B, x, y, z, 2, mc, f, g, fg, gg, {MD_U, MD_V, MD_QCZ}, gz);   // uz, vz, dQz
+    const double vx = gx[0], wx = gx[1], uy = gy[0], wy = gy[1], uz = gz[0], vz = gz[1];
+    o[0] = wy - vz;
+    o[vol] = uz - wx;
+    o[2 * vol] = vx - uy;
+    o[3 * vol] = sqrt((wy - vz) * (wy - vz) + (uz - wx) * (uz - wx) + (vx - uy) * (vx - uy));
+    o[4 * vol] = gx[2];
+    o[5 * vol] = gy[2];
+    o[6 * vol] = gz[2];
+}
+
+// ---- EB momentum-exchange force (Source/LBM.cpp:994-1044) -------------------
+// Each eb_boundary cell not covered by a finer level sums 2 e_q f(x - e_q, q)
+// over its fluid neighbours in FP64; the block reduces its cells' sums by warp
+// shuffles and a fixed tree over the warps and writes one partial per block,
+// and k_sum_partials adds the partials of all levels in a fixed order: the
+// result does not depend on the schedule (no atomics), run after run.
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(TILE_CELLS) k_eb_forces(LV L, const Tile* tiles, const double* f, const double* fg,
+                                                          double* partial3)
+{
+    __shared__ double red[3][TILE_CELLS / 32];
     int b, x, y, z;
     long long c;
     double fs[3] = {0.0, 0.0, 0.0};
@@ -62,8 +166,35 @@ __global__ void k_eb_forces(LV L, const Tile* tiles, const double* f, const doub
 #undef MBG_EB64
         }
     }
-    for (int d = 0; d < 3; ++d)
-        if (fs[d] != 0.0) atomicAdd(&out3[d], fs[d]);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int d = 0; d < 3; ++d) {
+        const double v = warp_sum(fs[d]);
+        if (lane == 0) red[d][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double s = 0.0;
+        for (int w = 0; w < TILE_CELLS / 32; ++w) s += red[threadIdx.x][w];
+        partial3[(long long)blockIdx.x * 3 + threadIdx.x] = s;
+    }
+}
+
+// out3 = sum of n partials (3 components each), in a fixed order: each of
+// the 256 threads sums a fixed strided subset, then a fixed tree
+__global__ void __launch_bounds__(256) k_sum_partials(const double* partial3, long long n, double* out3)
+{
+    __shared__ double red[3][256];
+    double s[3] = {0.0, 0.0, 0.0};
+    for (long long i = threadIdx.x; i < n; i += 256)
+        for (int d = 0; d < 3; ++d) s[d] += partial3[i * 3 + d];
+    for (int d = 0; d < 3; ++d) red[d][threadIdx.x] = s[d];
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            for (int d = 0; d < 3; ++d) red[d][threadIdx.x] += red[d][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) out3[threadIdx.x] = red[threadIdx.x][0];
 }
 
 
@@ -118,10 +249,22 @@ void launch_conserved(const LevelPlan& lp, const Phys64& ph, const double* f, co
     if (lp.ntiles > 0) k_conserved<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, ph, lp.tiles, f, g, dV, out5);
 }
 
-void launch_eb_forces(const LevelPlan& lp, const double* f, const double* fg, double* out3, cudaStream_t s)
+void launch_eb_forces(const LevelPlan& lp, const double* f, const double* fg, double* partial3, cudaStream_t s)
 {
     if (lp.ntiles == 0) return;
-    k_eb_forces<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, lp.tiles, f, fg, out3);
+    k_eb_forces<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, lp.tiles, f, fg, partial3);
+}
+
+void launch_sum_partials(const double* partial3, long long n, double* out3, cudaStream_t s)
+{
+    k_sum_partials<<<1, 256, 0, s>>>(partial3, n, out3);
+}
+
+void launch_derived(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, const double* fg,
+                    const double* gg, double* out7, cudaStream_t s)
+{
+    if (lp.ntiles == 0) return;
+    k_derived<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, ph, lp.tiles, f, g, fg, gg, out7);
 }
 
 }  // namespace mbg

@@ -98,7 +98,13 @@ void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParam
                      const double* gcAg, double* fcB, double* gcB, int into_state, cudaStream_t s);
 void launch_macro_local(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, double* out19,
                         cudaStream_t s);
-void launch_eb_forces(const LevelPlan& lp, const double* f, const double* fg, double* out3, cudaStream_t s);
+// per-block partial force sums (3 per tile) of one level; launch_sum_partials
+// adds n partials in a fixed order into out3
+void launch_eb_forces(const LevelPlan& lp, const double* f, const double* fg, double* partial3, cudaStream_t s);
+void launch_sum_partials(const double* partial3, long long n, double* out3, cudaStream_t s);
+// vorticity and q-correction gradients of the stored state, [box][7][cell]
+void launch_derived(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, const double* fg,
+                    const double* gg, double* out7, cudaStream_t s);
 void launch_conserved(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, double dV, double* out5,
                       cudaStream_t s);
 

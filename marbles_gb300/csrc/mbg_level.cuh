@@ -227,6 +227,33 @@ __device__ R bc_value(const LevelView<S>& L, const BCParams& P, const DevBox& B,
             if (is_g) return (R)eq_g_plain<double>(q, rho, vel, Rg, temp, gamma, lat);
             return (R)eq_f_plain<double>(q, rho, vel, Rg * temp);
         }
+        case 3: {  // pressure (Source/BC.H:222-321, dispatched at 421-446)
+            int gp[3] = {B.lo[0] + s[0], B.lo[1] + s[1], B.lo[2] + s[2]};
+            double vel[3] = {0.0, 0.0, 0.0}, Rg = 1.0, temp = 1.0 / 3.0, gamma = 5.0 / 3.0, rho_bc = 1.0;
+            vel_bc_state(P, L.dhi, gp, rho_bc, vel, Rg, temp, gamma);
+            double vb[3] = {0.0, 0.0, 0.0};
+            if (is_g) {
+                // the energy lattice uses the fixed outlet density 1 (BC.H:438-441)
+                const double rho_bcout = 1.0;
+                vb[idir] = ndir * (1.0 - (rho_bcout) / rho_bc);
+                return (R)eq_g_plain<double>(q, rho_bc, vb, Rg, temp, gamma, lat);
+            }
+            // density leaving through the face and tangential to it, from the
+            // populations of the interior cell's neighbours that point back
+            // across the face or along it, in direction order
+            double rho_out = 0.0, rho_tan = 0.0;
+            for (int qq = 0; qq < NQ; ++qq) {
+                const int bq2 = opp(qq);
+                const int ei = idir == 0 ? ev_x(bq2) : (idir == 1 ? ev_y(bq2) : ev_z(bq2));
+                if (ei != -ndir && ei != 0) continue;
+                const double val =
+                    (double)dec(fab_value(L, B, tx + ev_x(qq), ty + ev_y(qq), tz + ev_z(qq), bq2, v, vg), bq2);
+                if (ei == -ndir) rho_out += 2.0 * val;
+                else rho_tan += 1.0 * val;
+            }
+            vb[idir] = ndir * (1.0 - (rho_out + rho_tan) / rho_bc);
+            return (R)eq_f_plain<double>(q, rho_bc, vb, Rg * temp);
+        }
         case 5: {  // outflow: data(iv + ndir e_idir, q)
             s[idir] += ndir;
             int gp[3] = {B.lo[0] + s[0], B.lo[1] + s[1], B.lo[2] + s[2]};

@@ -559,6 +559,15 @@ mbg_status lowp_get_state(LowpLevel& L, const LevelPlan& plan, const std::vector
     return MBG_OK;
 }
 
+void lowp_decode(LowpLevel& L, const LevelPlan& plan, int lat, double* dst, cudaStream_t s)
+{
+    LowpDev* D = dev_of(L);
+    ensure_k(L, plan, known_bc(L), D->with_override, s);
+    const u16* src = (const u16*)(lat ? L.g[L.cur] : L.f[L.cur]);
+    const LowpK* k = D->dk + L.cur;
+    LOWP16(L.precision == MBG_FP32C_BF16S, decode, k, plan.tiles, plan.ntiles, src, L.NV, dst, lat, s);
+}
+
 mbg_status lowp_macro(LowpLevel& L, const LevelPlan& plan, double* out19, cudaStream_t s, std::string& err)
 {
     if (plan.ntiles == 0) return MBG_OK;

@@ -47,6 +47,9 @@ mbg_status lowp_set_state(LowpLevel& L, const LevelPlan& plan, const std::vector
                           const double* g, cudaStream_t s, std::string& err);
 mbg_status lowp_get_state(LowpLevel& L, const LevelPlan& plan, const std::vector<DevBox>& hbox, double* f,
                           double* g, cudaStream_t s, std::string& err);
+// the stored populations of lattice lat (0: f, 1: g) decoded to FP64 into
+// dst, [q][NV] in the FP64 form's valid-cell layout (the plan's view64)
+void lowp_decode(LowpLevel& L, const LevelPlan& plan, int lat, double* dst, cudaStream_t s);
 mbg_status lowp_macro(LowpLevel& L, const LevelPlan& plan, double* out19, cudaStream_t s, std::string& err);
 // adds the level's conserved totals (FP64) to out5 on the device
 void lowp_conserved(LowpLevel& L, const LevelPlan& plan, double dV, double* out5, cudaStream_t s);

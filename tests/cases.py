@@ -92,9 +92,11 @@ def gaussian_pulse(nc=128, fine_lo=32, fine_hi=95, mgs=32, nu=0.01, amp=0.01, wi
 
 
 def sphere_channel(nx=64, ny=32, nz=32, radius=6.0, center=(20.0, 16.0, 16.0), mgs=16, nu=0.016,
-                   mach=0.0670820, levels=1, bc_lo=(2, 0, 0), bc_hi=(5, 0, 0), t0=1.0 / 3.0):
+                   mach=0.0670820, levels=1, bc_lo=(2, 0, 0), bc_hi=(5, 0, 0), t0=1.0 / 3.0, velbc="constant",
+                   normal_dir=1, tangential_dir=0):
     """Flow past a sphere: velocity inflow at x-lo, outflow at x-hi,
-    periodic in y and z, constant velocity BC with u = Mach * c_s."""
+    periodic in y and z, constant velocity BC with u = Mach * c_s (or the
+    Channel / Parabolic profiles of Source/VelocityBC.H)."""
     p = O.default_params()
     p.n_cell[:] = [nx, ny, nz]
     p.prob_lo[:] = [0.0] * 3
@@ -105,8 +107,10 @@ def sphere_channel(nx=64, ny=32, nz=32, radius=6.0, center=(20.0, 16.0, 16.0), m
     p.max_grid_size = mgs
     p.nu = nu
     p.alpha = nu
-    p.velbc_type = O.VBC_TYPES["constant"]
+    p.velbc_type = O.VBC_TYPES[velbc]
     p.vbc_dir = 0
+    p.vbc_normal_dir = normal_dir
+    p.vbc_tangential_dir = tangential_dir
     p.vbc_mach_ref = mach
     p.vbc_initial_temperature = t0
     p.ic_initial_temperature = t0

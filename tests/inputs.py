@@ -42,7 +42,7 @@ lbm.ic_type = "gaussian_pulse"
 ic_gaussian_pulse.density = 1.0
 ic_gaussian_pulse.amplitude = 0.01
 ic_gaussian_pulse.width = {width}
-ic_gaussian_pulse.initial_temperature = 0.3333333333333333
+ic_gaussian_pulse.initial_temperature = {t0!r}
 tagging.refinement_indicators = centre
 tagging.centre.in_box_lo = {lo}.0 {lo}.0 {lo}.0
 tagging.centre.in_box_hi = {hi}.0 {hi}.0 {hi}.0
@@ -50,8 +50,8 @@ eb2.geom_type = "all_regular"
 """
 
 
-def pulse(nc=128, lo=32, hi=96, mgs=32, width=8.0):
-    return PULSE.format(nc=nc, lo=lo, hi=hi, mgs=mgs, width=width)
+def pulse(nc=128, lo=32, hi=96, mgs=32, width=8.0, t0=1.0 / 3.0):
+    return PULSE.format(nc=nc, lo=lo, hi=hi, mgs=mgs, width=width, t0=t0)
 
 
 SPHERE = """
