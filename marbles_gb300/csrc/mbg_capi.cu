@@ -52,6 +52,11 @@ struct Level {
     double* gqc = nullptr;
     Tile* d_tiles = nullptr;
     int ntiles = 0;
+    NbrSlot* d_slots = nullptr;
+    Tile* d_fast_tiles = nullptr;
+    int nfast = 0;
+    Tile* d_gen_tiles = nullptr;
+    int ngen = 0;
     GhostCell* d_ghost = nullptr;
     GhostCell* d_ghost1 = nullptr;
     long long nghost = 0, nghost1 = 0;
@@ -228,6 +233,68 @@ static int owner_host(const Level& L, const int p[3])
     return L.omap[((size_t)bk * L.nb[1] + bj) * L.nb[0] + bi];
 }
 
+// The 27 neighbour regions of every box (NbrSlot): a region maps to one box
+// when all its cells (after the periodic wrap) lie in that box's valid
+// cells at one fixed offset, or to the box's ghost fab when none lies in a
+// box and the box has one; ghost = -1 marks a region that maps to neither
+// (a non-periodic domain side, several boxes, covered and uncovered cells).
+static void build_slots(const Level& L, const int* is_periodic, std::vector<NbrSlot>& out)
+{
+    const int nbox = (int)L.boxes.size();
+    out.assign((size_t)nbox * 27, NbrSlot{0, 0, 0, -1, 0});
+    for (int n = 0; n < nbox; ++n) {
+        const HBox& b = L.boxes[n];
+        const DevBox& B = L.hbox[n];
+        for (int oz = 0; oz < 3; ++oz)
+            for (int oy = 0; oy < 3; ++oy)
+                for (int ox = 0; ox < 3; ++ox) {
+                    const int o3[3] = {ox, oy, oz};
+                    int rlo[3], rhi[3];
+                    for (int d = 0; d < 3; ++d) {
+                        rlo[d] = o3[d] == 0 ? -1 : (o3[d] == 1 ? 0 : b.n(d));
+                        rhi[d] = o3[d] == 0 ? -1 : (o3[d] == 1 ? b.n(d) - 1 : b.n(d));
+                    }
+                    int owner = -2;         // -2: unset, -1: uncovered
+                    int delta[3] = {0, 0, 0};
+                    bool ok = true;
+                    for (int z = rlo[2]; z <= rhi[2] && ok; ++z)
+                        for (int y = rlo[1]; y <= rhi[1] && ok; ++y)
+                            for (int x = rlo[0]; x <= rhi[0] && ok; ++x) {
+                                int gp[3] = {b.lo[0] + x, b.lo[1] + y, b.lo[2] + z};
+                                if (!wrap_host(L, is_periodic, gp)) { ok = false; break; }
+                                const int o = owner_host(L, gp);
+                                int dl[3] = {0, 0, 0};
+                                if (o >= 0) {
+                                    const int loc[3] = {gp[0] - L.boxes[o].lo[0], gp[1] - L.boxes[o].lo[1],
+                                                        gp[2] - L.boxes[o].lo[2]};
+                                    dl[0] = loc[0] - x; dl[1] = loc[1] - y; dl[2] = loc[2] - z;
+                                }
+                                if (owner == -2) {
+                                    owner = o;
+                                    for (int d = 0; d < 3; ++d) delta[d] = dl[d];
+                                } else if (o != owner || dl[0] != delta[0] || dl[1] != delta[1] || dl[2] != delta[2]) {
+                                    ok = false;
+                                }
+                            }
+                    NbrSlot& S = out[(size_t)n * 27 + ox + 3 * oy + 9 * oz];
+                    if (!ok) continue;
+                    if (owner >= 0) {
+                        const DevBox& O = L.hbox[owner];
+                        S.base = O.voff + (long long)delta[2] * O.sz + (long long)delta[1] * O.sy + delta[0];
+                        S.sy = O.sy;
+                        S.sz = O.sz;
+                        S.ghost = 0;
+                    } else if (B.goff >= 0) {
+                        const int gx = B.n[0] + 6, gy = B.n[1] + 6;
+                        S.base = B.goff + 3LL * gy * gx + 3LL * gx + 3;
+                        S.sy = gx;
+                        S.sz = gx * gy;
+                        S.ghost = 1;
+                    }
+                }
+    }
+}
+
 static void refresh_plan(mbg_ctx* ctx, Level& L)
 {
     LevelView<double> v;
@@ -247,6 +314,11 @@ static void refresh_plan(mbg_ctx* ctx, Level& L)
     L.plan.view64 = v;
     L.plan.tiles = L.d_tiles;
     L.plan.ntiles = L.ntiles;
+    L.plan.slots = L.d_slots;
+    L.plan.fast_tiles = L.d_fast_tiles;
+    L.plan.nfast = L.nfast;
+    L.plan.gen_tiles = L.d_gen_tiles;
+    L.plan.ngen = L.ngen;
     L.plan.ghost_list = L.d_ghost;
     L.plan.nghost_cells = L.nghost;
     L.plan.ghost_list1 = L.d_ghost1;
@@ -603,12 +675,32 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     MBG_CUDA(cudaMemcpyAsync(L.d_omap, L.omap.data(), L.omap.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     if ((st = dalloc(ctx, &L.d_flags, L.hflags.size())) != MBG_OK) return st;
     MBG_CUDA(cudaMemcpyAsync(L.d_flags, L.hflags.data(), L.hflags.size(), cudaMemcpyHostToDevice, ctx->s));
-    std::vector<Tile> tiles;
-    for (int n = 0; n < nbox; ++n)
-        for (long long s = 0; s < L.boxes[n].vol(); s += TILE_CELLS) tiles.push_back(Tile{n, (int)s});
+    std::vector<Tile> tiles, fast_tiles, gen_tiles;
+    std::vector<NbrSlot> slots;
+    build_slots(L, p.is_periodic, slots);
+    for (int n = 0; n < nbox; ++n) {
+        bool simple = L.hbox[n].all_fluid != 0;
+        for (int k = 0; k < 27 && simple; ++k) simple = slots[(size_t)n * 27 + k].ghost >= 0;
+        for (long long s = 0; s < L.boxes[n].vol(); s += TILE_CELLS) {
+            tiles.push_back(Tile{n, (int)s});
+            (simple ? fast_tiles : gen_tiles).push_back(Tile{n, (int)s});
+        }
+    }
     L.ntiles = (int)tiles.size();
+    L.nfast = (int)fast_tiles.size();
+    L.ngen = (int)gen_tiles.size();
     if ((st = dalloc(ctx, &L.d_tiles, tiles.size())) != MBG_OK) return st;
     MBG_CUDA(cudaMemcpyAsync(L.d_tiles, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, ctx->s));
+    if ((st = dalloc(ctx, &L.d_fast_tiles, fast_tiles.size())) != MBG_OK) return st;
+    if ((st = dalloc(ctx, &L.d_gen_tiles, gen_tiles.size())) != MBG_OK) return st;
+    if ((st = dalloc(ctx, &L.d_slots, slots.size())) != MBG_OK) return st;
+    if (!fast_tiles.empty())
+        MBG_CUDA(cudaMemcpyAsync(L.d_fast_tiles, fast_tiles.data(), fast_tiles.size() * sizeof(Tile),
+                                 cudaMemcpyHostToDevice, ctx->s));
+    if (!gen_tiles.empty())
+        MBG_CUDA(cudaMemcpyAsync(L.d_gen_tiles, gen_tiles.data(), gen_tiles.size() * sizeof(Tile),
+                                 cudaMemcpyHostToDevice, ctx->s));
+    MBG_CUDA(cudaMemcpyAsync(L.d_slots, slots.data(), slots.size() * sizeof(NbrSlot), cudaMemcpyHostToDevice, ctx->s));
     L.nghost = (long long)ghosts.size();
     L.nghost1 = (long long)ghosts1.size();
     if ((st = dalloc(ctx, &L.d_ghost, ghosts.size())) != MBG_OK) return st;
@@ -819,7 +911,7 @@ static mbg_status advance(mbg_ctx* ctx, int lev)
         launch_collide(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], L.md, L.gqc,
                        ctx->s);
     });
-    ctx->launches += 2;
+    ctx->launches += 2 * fp64_step_launches(L.plan);
     MBG_CUDA(cudaGetLastError());
     L.cur = Bf;
     return MBG_OK;

@@ -2,7 +2,12 @@
 // arithmetic).  Compiled with -fmad=false so that every multiply and add is
 // rounded separately, as in the reference's CPU build.
 //
-// A level advance is two passes over the valid cells:
+// A level advance is two passes over the valid cells, each launched over two
+// tile lists: boxes whose neighbourhood is plain (all fluid, no physical
+// boundary within one cell, every neighbour region held by one box) pull by
+// a per-box table of 27 neighbour slots -- the same index arithmetic for
+// every cell, so warps do not diverge at box faces -- and the other boxes
+// through the general pull with its boundary cases:
 //   k_moments : pull-stream f and g (Source/LBM.cpp:558-604) and compute the
 //               macro fields (f_to_macrodata, LBM.cpp:810-906) into a scratch
 //               array;
@@ -18,15 +23,90 @@
 
 namespace mbg {
 
+// ---- pulls through the neighbour-slot map of the CTA's box -----------------
+// (boxes of the fast tile list: all fluid, no physical boundary within one
+// cell, every neighbour region in one box or in the box's ghost fab)
+template <int q>
+__device__ __forceinline__ double pull_slot(const NbrSlot* S, const DevBox& B, int x, int y, int z,
+                                            const double* v, const double* vg, long long N, long long NG)
+{
+    constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
+    const int sx = x - ex, sy = y - ey, sz = z - ez;
+    const int ox = ex == 0 ? 1 : (sx < 0 ? 0 : (sx < B.n[0] ? 1 : 2));
+    const int oy = ey == 0 ? 1 : (sy < 0 ? 0 : (sy < B.n[1] ? 1 : 2));
+    const int oz = ez == 0 ? 1 : (sz < 0 ? 0 : (sz < B.n[2] ? 1 : 2));
+    const NbrSlot& s = S[ox + 3 * oy + 9 * oz];
+    const long long i = s.base + (long long)sz * s.sz + (long long)sy * s.sy + sx;
+    return s.ghost ? vg[q * NG + i] : v[q * N + i];
+}
+
+// Q_corr component d at box-local neighbour (x, y, z) through the slot map
+// (the macro scratch has the layout of the populations; the ghost fab's
+// Q_corr scratch that of the ghost fab)
+__device__ __forceinline__ double qcorr_slot(const NbrSlot* S, const DevBox& B, int x, int y, int z, int d,
+                                             const double* md, const double* gqc, long long N, long long NG)
+{
+    const int ox = x < 0 ? 0 : (x < B.n[0] ? 1 : 2);
+    const int oy = y < 0 ? 0 : (y < B.n[1] ? 1 : 2);
+    const int oz = z < 0 ? 0 : (z < B.n[2] ? 1 : 2);
+    const NbrSlot& s = S[ox + 3 * oy + 9 * oz];
+    const long long i = s.base + (long long)z * s.sz + (long long)y * s.sy + x;
+    return s.ghost ? gqc[d * NG + i] : md[(MD_QCX + d) * N + i];
+}
+
+// gradient() of Source/Utilities.H:279-312 in an all-fluid box: one-sided
+// only at the domain box
+__device__ __forceinline__ double qgrad_slot(const LV& L, const NbrSlot* S, const DevBox& B, int x, int y, int z,
+                                             int d, double idx, const double* md, const double* gqc)
+{
+    int pp[3] = {x, y, z}, pm[3] = {x, y, z};
+    pp[d] += 1;
+    pm[d] -= 1;
+    const bool p_out = B.lo[d] + pp[d] > L.dhi[d];
+    const bool m_out = B.lo[d] + pm[d] < L.dlo[d];
+    double vp = 0.0, vc = 0.0, vm = 0.0;
+    if (p_out && m_out) {
+        vp = 0.0; vc = 0.0; vm = 0.0;
+    } else if (p_out) {
+        vp = 0.0;
+        vc = qcorr_slot(S, B, x, y, z, d, md, gqc, L.N, L.NG);
+        vm = -qcorr_slot(S, B, pm[0], pm[1], pm[2], d, md, gqc, L.N, L.NG);
+    } else if (m_out) {
+        vp = qcorr_slot(S, B, pp[0], pp[1], pp[2], d, md, gqc, L.N, L.NG);
+        vc = -qcorr_slot(S, B, x, y, z, d, md, gqc, L.N, L.NG);
+        vm = 0.0;
+    } else {
+        vp = 0.5 * qcorr_slot(S, B, pp[0], pp[1], pp[2], d, md, gqc, L.N, L.NG);
+        vc = 0.0;
+        vm = -0.5 * qcorr_slot(S, B, pm[0], pm[1], pm[2], d, md, gqc, L.N, L.NG);
+    }
+    return (vp + vc + vm) * idx;
+}
+
+// the CTA's tile: its box's slot map in shared memory, the thread's cell
+template <bool FAST>
+__device__ __forceinline__ bool tile_setup(const LV& L, const LevelPlan& lp, const Tile* tiles, NbrSlot* sl, int& b,
+                                           int& x, int& y, int& z, long long& c)
+{
+    if (FAST) {
+        const int box = tiles[blockIdx.x].box;
+        if (threadIdx.x < 27) sl[threadIdx.x] = lp.slots[(long long)box * 27 + threadIdx.x];
+        __syncthreads();
+    }
+    return cell_of_tile(L, tiles, b, x, y, z, c);
+}
+
 // ---- pass 1: stream + macro fields ----------------------------------------
-__global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, BCParams P, Phys64 ph, const Tile* tiles,
+template <bool FAST>
+__global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, LevelPlan lp, BCParams P, Phys64 ph, const Tile* tiles,
                                                         const double* fA, const double* gA, const double* fAg,
                                                         const double* gAg, const double* fB, const double* gB,
                                                         double* md)
 {
+    __shared__ NbrSlot sl[27];
     int b, x, y, z;
     long long c;
-    if (!cell_of_tile(L, tiles, b, x, y, z, c)) return;
+    if (!tile_setup<FAST>(L, lp, tiles, sl, b, x, y, z, c)) return;
     const DevBox& B = L.box[b];
     const uint8_t tf = flag_at(L, B, x, y, z);
     if (!(tf & FL_FLUID)) return;
@@ -34,14 +114,16 @@ __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, BCParams P, Phys64
     const bool interior = !ovr && is_interior(B, x, y, z);
     const long long cell = B.voff + c;
     MomentAcc<double> acc;
+#define MBG_PULLF(q) (FAST ? pull_slot<q>(sl, B, x, y, z, fA, fAg, L.N, L.NG) \
+                           : pull<q>(L, P, B, x, y, z, tf, interior, fA, fAg, false, ph.lat))
+#define MBG_PULLG(q) (FAST ? pull_slot<q>(sl, B, x, y, z, gA, gAg, L.N, L.NG) \
+                           : pull<q>(L, P, B, x, y, z, tf, interior, gA, gAg, true, ph.lat))
 #define MBG_M64(q)                                                             \
     {                                                                          \
         double fq = ovr ? fB[q * L.N + cell] : 0.0;                            \
         double gq = ovr ? gB[q * L.N + cell] : 0.0;                            \
-        if (!ovr || is_noovr(fq))                                              \
-            fq = pull<q>(L, P, B, x, y, z, tf, interior, fA, fAg, false, ph.lat); \
-        if (!ovr || is_noovr(gq))                                              \
-            gq = pull<q>(L, P, B, x, y, z, tf, interior, gA, gAg, true, ph.lat);  \
+        if (!ovr || is_noovr(fq)) fq = MBG_PULLF(q);                           \
+        if (!ovr || is_noovr(gq)) gq = MBG_PULLG(q);                           \
         acc.template add<q>(fq, gq);                                           \
     }
     MBG_UNROLL27(MBG_M64)
@@ -69,14 +151,16 @@ __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, BCParams P, Phys64
 }
 
 // ---- pass 2: q-correction, equilibria, relaxation --------------------------
-__global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, BCParams P, Phys64 ph, const Tile* tiles,
+template <bool FAST>
+__global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, LevelPlan lp, BCParams P, Phys64 ph, const Tile* tiles,
                                                         const double* fA, const double* gA, const double* fAg,
                                                         const double* gAg, double* fB, double* gB,
                                                         const double* md, const double* gqc)
 {
+    __shared__ NbrSlot sl[27];
     int b, x, y, z;
     long long c;
-    if (!cell_of_tile(L, tiles, b, x, y, z, c)) return;
+    if (!tile_setup<FAST>(L, lp, tiles, sl, b, x, y, z, c)) return;
     const DevBox& B = L.box[b];
     const uint8_t tf = flag_at(L, B, x, y, z);
     const long long N = L.N;
@@ -108,23 +192,30 @@ __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, BCParams P, Phys64
     m.qy = md[MD_QY * N + cell];
     m.qz = md[MD_QZ * N + cell];
     m.temp = md[MD_T * N + cell];
-    const double dqx = qgrad(L, B, x, y, z, 0, ph.idx[0], md, gqc);
-    const double dqy = qgrad(L, B, x, y, z, 1, ph.idx[1], md, gqc);
-    const double dqz = qgrad(L, B, x, y, z, 2, ph.idx[2], md, gqc);
+    double dqx, dqy, dqz;
+    if (FAST) {
+        dqx = qgrad_slot(L, sl, B, x, y, z, 0, ph.idx[0], md, gqc);
+        dqy = qgrad_slot(L, sl, B, x, y, z, 1, ph.idx[1], md, gqc);
+        dqz = qgrad_slot(L, sl, B, x, y, z, 2, ph.idx[2], md, gqc);
+    } else {
+        dqx = qgrad(L, B, x, y, z, 0, ph.idx[0], md, gqc);
+        dqy = qgrad(L, B, x, y, z, 1, ph.idx[1], md, gqc);
+        dqz = qgrad(L, B, x, y, z, 2, ph.idx[2], md, gqc);
+    }
     Equilibrium<double> E;
     const double omega =
         build_equilibrium<double>(m, dqx, dqy, dqz, ph.nu, ph.alpha, ph.dt, ph.Rg, ph.cv, ph.lat, E);
 #define MBG_RF64(q)                                                                                  \
     {                                                                                                \
         double fq = ovr ? fB[q * N + cell] : 0.0;                                                    \
-        if (!ovr || is_noovr(fq)) fq = pull<q>(L, P, B, x, y, z, tf, interior, fA, fAg, false, ph.lat); \
+        if (!ovr || is_noovr(fq)) fq = MBG_PULLF(q);                                                 \
         const double feq = E.template feq<q>();                                                      \
         fB[q * N + cell] = fq + omega * (feq - fq);                                                  \
     }
 #define MBG_RG64(q)                                                                                  \
     {                                                                                                \
         double gq = ovr ? gB[q * N + cell] : 0.0;                                                    \
-        if (!ovr || is_noovr(gq)) gq = pull<q>(L, P, B, x, y, z, tf, interior, gA, gAg, true, ph.lat); \
+        if (!ovr || is_noovr(gq)) gq = MBG_PULLG(q);                                                 \
         const double geq = E.template geq<q>(ph.lat);                                                \
         gB[q * N + cell] = gq + omega * (geq - gq);                                                  \
     }
@@ -132,23 +223,36 @@ __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, BCParams P, Phys64
     MBG_UNROLL27(MBG_RG64)
 #undef MBG_RF64
 #undef MBG_RG64
+#undef MBG_PULLF
+#undef MBG_PULLG
 }
 
 // ---- launchers -----------------------------------------------------------
+// the fast tiles through the slot maps, the others through the general pull
 void launch_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
                     const double* fAg, const double* gAg, const double* fB, const double* gB, double* md,
                     cudaStream_t s)
 {
-    if (lp.ntiles == 0) return;
-    k_moments<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, P, ph, lp.tiles, fA, gA, fAg, gAg, fB, gB, md);
+    if (lp.nfast > 0)
+        k_moments<true><<<lp.nfast, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB,
+                                                       gB, md);
+    if (lp.ngen > 0)
+        k_moments<false><<<lp.ngen, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB,
+                                                        gB, md);
 }
 
 void launch_collide(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
                     const double* fAg, const double* gAg, double* fB, double* gB, const double* md,
                     const double* gqc, cudaStream_t s)
 {
-    if (lp.ntiles == 0) return;
-    k_collide<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, P, ph, lp.tiles, fA, gA, fAg, gAg, fB, gB, md, gqc);
+    if (lp.nfast > 0)
+        k_collide<true><<<lp.nfast, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB,
+                                                       gB, md, gqc);
+    if (lp.ngen > 0)
+        k_collide<false><<<lp.ngen, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB,
+                                                        gB, md, gqc);
 }
+
+int fp64_step_launches(const LevelPlan& lp) { return (lp.nfast > 0) + (lp.ngen > 0); }
 
 }  // namespace mbg

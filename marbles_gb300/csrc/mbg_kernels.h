@@ -59,10 +59,31 @@ struct Phys32 {
     float inv_fscale, inv_gscale;
 };
 
+// One of the 27 neighbour regions of a box (index ox + 3 oy + 9 oz, o = 0
+// below, 1 inside, 2 above the box along each axis; 13 is the box itself):
+// the storage of the cells there as an affine map of box-local positions,
+// index = base + z sz + y sy + x, into the valid cells of the level (stride
+// N) or into the box's own ghost fab (stride NG).
+struct NbrSlot {
+    long long base;
+    int sy, sz;
+    int ghost;
+    int pad;
+};
+
 struct LevelPlan {
     LevelView<double> view64;
     const Tile* tiles = nullptr;
     int ntiles = 0;
+    // FP64 form: the tiles of boxes whose 27 neighbour regions each map to one
+    // box (or to the box's ghost fab), with no solid cell in the grown box and
+    // no non-periodic domain side within one cell -- their pulls are the slot
+    // maps above -- and the tiles of the other boxes (general pull)
+    const NbrSlot* slots = nullptr;   // [box][27]
+    const Tile* fast_tiles = nullptr;
+    int nfast = 0;
+    const Tile* gen_tiles = nullptr;
+    int ngen = 0;
     const GhostCell* ghost_list = nullptr;   // all uncovered ghost cells
     long long nghost_cells = 0;
     const GhostCell* ghost_list1 = nullptr;  // first ghost layer only
@@ -85,6 +106,8 @@ void launch_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, co
 void launch_collide(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
                     const double* fAg, const double* gAg, double* fB, double* gB, const double* md,
                     const double* gqc, cudaStream_t s);
+// kernel launches of one launch_moments or launch_collide call
+int fp64_step_launches(const LevelPlan& lp);
 void launch_ghost_stream(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA,
                          const double* gA, const double* fAg, const double* gAg, double* fBg, double* gBg,
                          cudaStream_t s);

@@ -52,13 +52,15 @@ def test_create_rejects_inconsistent_periodicity():
         M.Context(p)
 
 
-def test_create_rejects_pressure_bc():
+def test_create_rejects_pressure_bc_beside_walls():
+    """A pressure face needs periodic tangential directions (the reference's
+    functor result depends on its visiting order next to other walls)."""
     import marbles_gb300 as M
     p = M.default_params()
-    p.is_periodic[:] = [0, 1, 1]
-    p.bc_lo[:] = [3, 0, 0]
-    p.bc_hi[:] = [5, 0, 0]
-    with pytest.raises(M.MbgError, match="pressure"):
+    p.is_periodic[:] = [0, 0, 1]
+    p.bc_lo[:] = [3, 1, 0]
+    p.bc_hi[:] = [5, 1, 0]
+    with pytest.raises(M.MbgError, match="periodic tangential"):
         M.Context(p)
 
 
