@@ -152,7 +152,7 @@ mbg_status mbg_average_down(mbg_ctx* ctx, int crse_lev, int crse_ng);
  * (cells not covered by a finer level), FP64 accumulation in a fixed order
  * (per-block sums by warp shuffles, then one fixed-order sum of the blocks):
  * the same state gives the same bits on every call.  16-bit forms: the
- * stored populations decoded to FP64 (ghost fabs of fine levels excluded).
+ * stored populations (and fine levels' ghost fabs) decoded to FP64.
  * Replaces LBM::compute_eb_forces (Source/LBM.cpp:994-1044). */
 mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3]);
 
@@ -291,6 +291,41 @@ void mbg_adj_destroy(mbg_adj* a);
 #define MBG_NOALLOC_MAX_CELLS 32768
 mbg_status mbg_step_box_noalloc(const mbg_params* params, const double* f_in, const double* g_in,
                                 double* f_out, double* g_out, void* cuda_stream);
+
+/* ---- embedded-boundary geometry -------------------------------------------
+ * eb2.geom_type and its keys (Source/EB.cpp:5-38, Source/Geometry.cpp:5-200):
+ * the AMReX built-in sphere, box, cylinder and plane and the reference's own
+ * rotated box, rotated cylinder and extruded triangles. */
+enum {
+    MBG_GEOM_ALL_REGULAR = 0, MBG_GEOM_SPHERE = 1, MBG_GEOM_BOX = 2, MBG_GEOM_CYLINDER = 3,
+    MBG_GEOM_PLANE = 4, MBG_GEOM_ROTATED_BOX = 5, MBG_GEOM_ROTATED_CYLINDER = 6,
+    MBG_GEOM_EXTRUDED_TRIANGLES = 7
+};
+typedef struct mbg_geometry {
+    int type;                   /* MBG_GEOM_*                                       */
+    int has_fluid_inside;       /* eb2.{sphere,box,cylinder}_has_fluid_inside       */
+    double center[3];           /* eb2.sphere_center / eb2.cylinder_center          */
+    double radius;              /* eb2.sphere_radius / eb2.cylinder_radius          */
+    double height;              /* eb2.cylinder_height (<= 0: unbounded)            */
+    int direction;              /* eb2.cylinder_direction                           */
+    double lo[3], hi[3];        /* eb2.box_lo, eb2.box_hi                           */
+    double point[3], normal[3]; /* eb2.plane_point, eb2.plane_normal                */
+    double rotation_deg;        /* eb2.box_rotation / eb2.cylinder_rotation         */
+    int rotation_axis;          /* eb2.box_rotation_axe / eb2.cylinder_rotation_axe */
+    double rotation_center[3];  /* eb2.box_rotation_center                          */
+    int ntri;                   /* extruded_triangles.num_tri (at most 5)           */
+    double tri[5][3][2];        /* extruded_triangles.tri_<t>_point_<p> (x, y)      */
+} mbg_geometry;
+
+/* is_fluid flags (bit 0 is_fluid, bit 1 eb_boundary) of level lev's boxes,
+ * each grown by 3, in the layout mbg_define_level takes, evaluated on the
+ * GPU on cuda_stream: a cell is covered when the geometry's implicit
+ * function puts all 8 of its corners in the body.  Uses params' n_cell,
+ * prob_lo/hi and is_periodic.  Replaces the EB2 build and
+ * initialize_is_fluid (Source/EB.cpp:5-38, Source/LBM.cpp:1213-1262).
+ * Errors are reported by mbg_last_error(NULL). */
+mbg_status mbg_geometry_flags(const mbg_geometry* geom, const mbg_params* params, int lev, int nbox,
+                              const int* lohi, uint8_t* flags, void* cuda_stream);
 
 /* ---- AMReX-format files (host only, no device work) ------------------------
  * Errors are reported by mbg_last_error(NULL).

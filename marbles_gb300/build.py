@@ -31,6 +31,7 @@ UNITS = {
     "lbm_driver.cu": [],
     "lbm_capi.cu": [],
     "lbm_io.cu": [],
+    "mbg_geometry.cu": ["-fmad=false"],
     "mbg_noalloc.cu": ["-fmad=false"],
 }
 EXE = os.path.join(HERE, "marbles_gb300_run")

@@ -14,6 +14,7 @@
 #include <sys/stat.h>
 
 #include "lbm_driver.h"
+#include "mbg_geometry.cuh"
 #include "mbg_physics.cuh"
 
 namespace mbgdrv {
@@ -272,16 +273,79 @@ bool LBM::configure(const Inputs& in, std::string& e)
     else { e = "lbm.precision must be fp64, fp16 or bf16"; return false; }
     // eb2.*
     in.query("eb2.geom_type", c.geom_type);
-    if (c.geom_type == "sphere") {
-        in.query("eb2.sphere_radius", c.sphere_radius);
-        if (!need3(in, "eb2.sphere_center", dv, e)) return false;
-        for (int d = 0; d < 3; ++d) c.sphere_center[d] = dv[d];
+    {
+        // Source/EB.cpp:5-38 (AMReX built-ins) and Source/Geometry.cpp:5-200
+        mbg_geometry& g = c.geom;
+        std::memset(&g, 0, sizeof g);
+        g.height = -1.0;
+        g.normal[0] = 1.0;
+        const std::string& t = c.geom_type;
+        auto get3 = [&](const std::string& key, double* out, bool required) -> bool {
+            std::vector<double> v;
+            if (!in.queryarr(key, v) || v.size() < 3) {
+                if (required) e = key + " must have 3 entries";
+                return !required;
+            }
+            for (int d = 0; d < 3; ++d) out[d] = v[d];
+            return true;
+        };
         bool inside = false;
-        in.query("eb2.sphere_has_fluid_inside", inside);
-        c.sphere_has_fluid_inside = inside;
-    } else if (c.geom_type != "all_regular") {
-        e = "eb2.geom_type '" + c.geom_type + "' is not supported (all_regular, sphere)";
-        return false;
+        if (t == "all_regular") {
+            g.type = MBG_GEOM_ALL_REGULAR;
+        } else if (t == "sphere") {
+            g.type = MBG_GEOM_SPHERE;
+            in.query("eb2.sphere_radius", g.radius);
+            if (!get3("eb2.sphere_center", g.center, true)) return false;
+            in.query("eb2.sphere_has_fluid_inside", inside);
+        } else if (t == "box" || t == "rotated_box") {
+            g.type = t == "box" ? MBG_GEOM_BOX : MBG_GEOM_ROTATED_BOX;
+            if (!get3("eb2.box_lo", g.lo, true) || !get3("eb2.box_hi", g.hi, true)) return false;
+            in.query("eb2.box_has_fluid_inside", inside);
+            in.query("eb2.box_rotation", g.rotation_deg);
+            in.query("eb2.box_rotation_axe", g.rotation_axis);
+            get3("eb2.box_rotation_center", g.rotation_center, false);
+        } else if (t == "cylinder" || t == "rotated_cylinder") {
+            g.type = t == "cylinder" ? MBG_GEOM_CYLINDER : MBG_GEOM_ROTATED_CYLINDER;
+            if (t == "rotated_cylinder") {   // RotatedCylinder's defaults (Geometry.cpp:131-136)
+                g.radius = 0.0002;
+                inside = true;
+            }
+            in.query("eb2.cylinder_radius", g.radius);
+            in.query("eb2.cylinder_direction", g.direction);
+            if (t == "cylinder") in.query("eb2.cylinder_height", g.height);
+            if (!get3("eb2.cylinder_center", g.center, true)) return false;
+            in.query("eb2.cylinder_has_fluid_inside", inside);
+            in.query("eb2.cylinder_rotation", g.rotation_deg);
+            in.query("eb2.cylinder_rotation_axe", g.rotation_axis);
+        } else if (t == "plane") {
+            g.type = MBG_GEOM_PLANE;
+            if (!get3("eb2.plane_point", g.point, true) || !get3("eb2.plane_normal", g.normal, true)) return false;
+        } else if (t == "extruded_triangles") {
+            g.type = MBG_GEOM_EXTRUDED_TRIANGLES;
+            if (!in.query("extruded_triangles.num_tri", g.ntri) || g.ntri < 0 || g.ntri > 5) {
+                e = "extruded_triangles.num_tri must be 0 .. 5";
+                return false;
+            }
+            for (int tri = 0; tri < g.ntri; ++tri)
+                for (int pt = 0; pt < 3; ++pt) {
+                    double v[3];
+                    const std::string key =
+                        "extruded_triangles.tri_" + std::to_string(tri) + "_point_" + std::to_string(pt);
+                    if (!get3(key, v, true)) return false;
+                    g.tri[tri][pt][0] = v[0];
+                    g.tri[tri][pt][1] = v[1];
+                }
+        } else {
+            e = "eb2.geom_type '" + t + "' is not supported (all_regular, sphere, box, cylinder, plane, "
+                "rotated_box, rotated_cylinder, extruded_triangles)";
+            return false;
+        }
+        g.has_fluid_inside = inside ? 1 : 0;
+        if (g.direction < 0 || g.direction > 2 || g.rotation_axis < 0 || g.rotation_axis > 2) {
+            e = "eb2: cylinder_direction and the rotation axis must be 0, 1 or 2";
+            return false;
+        }
+        geom_ = mbg::geom_from(g);
     }
     // tagging.* (LBM.cpp:302-396)
     std::vector<std::string> inds;
@@ -393,20 +457,9 @@ void LBM::level_geometry(int lev, double dx[3]) const
 
 bool LBM::covered_cell(int lev, int i, int j, int k) const
 {
-    if (cfg_.geom_type != "sphere") return false;
     double dx[3];
     level_geometry(lev, dx);
-    const double r2 = cfg_.sphere_radius * cfg_.sphere_radius;
-    const double sgn = cfg_.sphere_has_fluid_inside ? -1.0 : 1.0;
-    for (int c = 0; c < 8; ++c) {
-        const double x = cfg_.prob_lo[0] + (i + (c & 1)) * dx[0];
-        const double y = cfg_.prob_lo[1] + (j + ((c >> 1) & 1)) * dx[1];
-        const double z = cfg_.prob_lo[2] + (k + ((c >> 2) & 1)) * dx[2];
-        const double ax = x - cfg_.sphere_center[0], ay = y - cfg_.sphere_center[1], az = z - cfg_.sphere_center[2];
-        const double phi = sgn * (r2 - (ax * ax + ay * ay + az * az));
-        if (!(phi >= 0.0)) return false;
-    }
-    return true;
+    return mbg::geom_covered(geom_, cfg_.prob_lo, dx, i, j, k);
 }
 
 namespace {
@@ -461,7 +514,7 @@ void LBM::make_flags(int lev)
     };
     std::vector<uint8_t>& out = flags_[lev];
     out.clear();
-    const bool regular = cfg_.geom_type == "all_regular";
+    const bool regular = geom_.type == mbg::GEOM_ALL_REGULAR;
     for (const Box& b : ba) {
         for (int k = b.lo[2] - 3; k <= b.hi[2] + 3; ++k)
             for (int j = b.lo[1] - 3; j <= b.hi[1] + 3; ++j)
@@ -794,6 +847,11 @@ mbg_status LBM::init_data()
         std::vector<int> lohi;
         for (const Box& b : grids_[lev])
             for (int x : {b.lo[0], b.lo[1], b.lo[2], b.hi[0], b.hi[1], b.hi[2]}) lohi.push_back(x);
+        // the level's is_fluid flags from the geometry, on the GPU (the grids
+        // above were tagged from the same implicit functions on the host)
+        st = mbg_geometry_flags(&cfg_.geom, &p, (int)lev, (int)grids_[lev].size(), lohi.data(), flags_[lev].data(),
+                                mbg_stream(ctx_));
+        if (st != MBG_OK) { err = mbg_last_error(nullptr); return st; }
         st = mbg_define_level(ctx_, (int)lev, (int)grids_[lev].size(), lohi.data(), flags_[lev].data());
         if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
         if (!cfg_.restart.empty()) continue;

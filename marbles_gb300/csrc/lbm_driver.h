@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/marbles_gb300.h"
+#include "mbg_geometry.cuh"
 
 namespace mbgdrv {
 
@@ -70,10 +71,9 @@ struct Config {
     bool save_streaming = true, save_derived = true, compute_forces = false;
     std::string forces_file = "forces.txt";
     double initial_temperature = 1.0 / 3.0, adiabatic_exponent = 5.0 / 3.0, m_bar = 28.96;
-    // eb2.*
+    // eb2.* (and extruded_triangles.*)
     std::string geom_type = "all_regular";
-    double sphere_radius = 0.0, sphere_center[3] = {0, 0, 0};
-    int sphere_has_fluid_inside = 0;
+    mbg_geometry geom{};
     // tagging.*
     struct Tag {
         std::string name;
@@ -135,6 +135,7 @@ public:
 
 private:
     Config cfg_;
+    mbg::GeomDesc geom_;   // implicit function of cfg_.geom (host evaluation)
     ICParams ic_;
     VelBC vbc_;
     mbg_ctx* ctx_ = nullptr;

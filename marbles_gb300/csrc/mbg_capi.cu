@@ -113,6 +113,8 @@ struct mbg_ctx {
     // FP64 decode of a 16-bit level's f and g for the output kernels
     double* d_dec[2] = {nullptr, nullptr};
     size_t dec_n[2] = {0, 0};
+    double* d_decg[2] = {nullptr, nullptr};   // and of its ghost fabs
+    size_t decg_n[2] = {0, 0};
     std::vector<void*> allocs;
 };
 
@@ -1074,8 +1076,8 @@ mbg_status mbg_average_down(mbg_ctx* ctx, int crse_lev, int crse_ng)
 }
 
 // FP64 views of a level's stored populations for the output kernels: the
-// FP64 form's own buffers; the 16-bit forms' populations decoded into FP64
-// scratch of the context (f, and g when want_g), without their ghost fabs
+// FP64 form's own buffers; the 16-bit forms' populations and ghost fabs
+// decoded into FP64 scratch of the context (f, and g when want_g)
 static mbg_status fp64_state(mbg_ctx* ctx, Level& L, bool want_g, const double** f, const double** g,
                              const double** fg, const double** gg)
 {
@@ -1086,20 +1088,29 @@ static mbg_status fp64_state(mbg_ctx* ctx, Level& L, bool want_g, const double**
         *gg = L.gg[L.cur];
         return MBG_OK;
     }
-    const size_t need = (size_t)L.N * NQ;
+    const size_t need = (size_t)L.N * NQ, needg = (size_t)L.NG * NQ;
     for (int lat = 0; lat < (want_g ? 2 : 1); ++lat) {
         if (ctx->dec_n[lat] < need) {
             mbg_status st = dalloc(ctx, &ctx->d_dec[lat], need);
             if (st != MBG_OK) return st;
             ctx->dec_n[lat] = need;
         }
+        if (ctx->decg_n[lat] < needg) {
+            mbg_status st = dalloc(ctx, &ctx->d_decg[lat], needg);
+            if (st != MBG_OK) return st;
+            ctx->decg_n[lat] = needg;
+        }
         lowp_decode(L.lowp, L.plan, lat, ctx->d_dec[lat], ctx->s);
         ctx->launches++;
+        if (needg > 0) {
+            lowp_decode_ghost(L.lowp, L.plan, lat, ctx->d_decg[lat], ctx->s);
+            ctx->launches++;
+        }
     }
     *f = ctx->d_dec[0];
     *g = want_g ? ctx->d_dec[1] : nullptr;
-    *fg = nullptr;
-    *gg = nullptr;
+    *fg = needg > 0 ? ctx->d_decg[0] : nullptr;
+    *gg = needg > 0 && want_g ? ctx->d_decg[1] : nullptr;
     return MBG_OK;
 }
 

@@ -568,6 +568,16 @@ void lowp_decode(LowpLevel& L, const LevelPlan& plan, int lat, double* dst, cuda
     LOWP16(L.precision == MBG_FP32C_BF16S, decode, k, plan.tiles, plan.ntiles, src, L.NV, dst, lat, s);
 }
 
+void lowp_decode_ghost(LowpLevel& L, const LevelPlan& plan, int lat, double* dst, cudaStream_t s)
+{
+    if (L.NG <= 0) return;
+    LowpDev* D = dev_of(L);
+    ensure_k(L, plan, known_bc(L), D->with_override, s);
+    const u16* src = (const u16*)(lat ? L.gg[L.cur] : L.fg[L.cur]);
+    const LowpK* k = D->dk + L.cur;
+    LOWP16(L.precision == MBG_FP32C_BF16S, decode_flat, k, src, L.NG, dst, lat, s);
+}
+
 mbg_status lowp_macro(LowpLevel& L, const LevelPlan& plan, double* out19, cudaStream_t s, std::string& err)
 {
     if (plan.ntiles == 0) return MBG_OK;

@@ -50,6 +50,8 @@ mbg_status lowp_get_state(LowpLevel& L, const LevelPlan& plan, const std::vector
 // the stored populations of lattice lat (0: f, 1: g) decoded to FP64 into
 // dst, [q][NV] in the FP64 form's valid-cell layout (the plan's view64)
 void lowp_decode(LowpLevel& L, const LevelPlan& plan, int lat, double* dst, cudaStream_t s);
+// the ghost fabs of lattice lat decoded to FP64 into dst, [q][NG] (fine levels)
+void lowp_decode_ghost(LowpLevel& L, const LevelPlan& plan, int lat, double* dst, cudaStream_t s);
 mbg_status lowp_macro(LowpLevel& L, const LevelPlan& plan, double* out19, cudaStream_t s, std::string& err);
 // adds the level's conserved totals (FP64) to out5 on the device
 void lowp_conserved(LowpLevel& L, const LevelPlan& plan, double dV, double* out5, cudaStream_t s);

@@ -988,6 +988,16 @@ __global__ void k_decode16(const LowpK* __restrict__ K, const Tile* __restrict__
     for (int q = 0; q < NQ; ++q) dst[q * NV + hc] = (double)dec<BF>(K->ct, src[q * L.N + pc], q, isg != 0);
 }
 
+// a [q][n] array (a level's ghost fabs) decoded to FP64, value by value
+template <bool BF>
+__global__ void k_decode_flat16(const LowpK* __restrict__ K, const u16* __restrict__ src, long long n,
+                                double* __restrict__ dst, int isg)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * NQ) return;
+    dst[i] = (double)dec<BF>(K->ct, src[i], (int)(i / n), isg != 0);
+}
+
 // macro fields (host layout [box][19][cell]) in FP64 from the decoded state
 template <bool BF>
 __global__ void k_macro16(const LowpK* __restrict__ K, const CodecTab ct, const Tile* tiles, double* out19)
@@ -1170,6 +1180,11 @@ void Lowp16<BF>::decode(const LowpK* k, const Tile* tiles, int ntiles, const u16
                         int isg, cudaStream_t s)
 {
     if (ntiles > 0) k_decode16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, tiles, src, NV, dst, isg);
+}
+template <bool BF>
+void Lowp16<BF>::decode_flat(const LowpK* k, const u16* src, long long n, double* dst, int isg, cudaStream_t s)
+{
+    if (n > 0) k_decode_flat16<BF><<<(unsigned)((n * NQ + 255) / 256), 256, 0, s>>>(k, src, n, dst, isg);
 }
 template <bool BF>
 void Lowp16<BF>::conserved(const LowpK* k, const Tile* tiles, int ntiles, double dV, double* out5, cudaStream_t s)

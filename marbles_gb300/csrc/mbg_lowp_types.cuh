@@ -131,6 +131,8 @@ struct Lowp16 {
     static void macro(const LowpK* k, const CodecTab& ct, const Tile* tiles, int ntiles, double* out19,
                       cudaStream_t s);
     static void conserved(const LowpK* k, const Tile* tiles, int ntiles, double dV, double* out5, cudaStream_t s);
+    // every value of a [q][n] array (the ghost fabs) decoded to FP64
+    static void decode_flat(const LowpK* k, const u16* src, long long n, double* dst, int isg, cudaStream_t s);
 };
 extern template struct Lowp16<false>;
 extern template struct Lowp16<true>;

@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 import cases
+import inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -90,3 +91,47 @@ def test_batch_autotune_keeps_state():
     assert 0 <= v < 4 and all(t > 0 for t in ms)
     b.step(4)
     assert np.isfinite(b.get_state()[0]).all()
+
+
+def test_batch_256_literal_domains_against_fp64():
+    """The batched workload itself: all 256 Taylor-Green domains at their own
+    cell counts (16 ... 96 per axis), velocities and viscosities, advanced
+    2 steps by the FP16 batch against one FP64 context per domain (the FP64
+    form is bit-identical to the oracle on these domains,
+    test_parity_full.py).  Two steps: the literal viscosities at RT = 1/3 are
+    linearly unstable in the scheme (test_stability.py).  rho and T within
+    1e-4 / 1e-3 pointwise; u within 3e-3 of each domain's largest velocity
+    (FP16 keeps 11 bits of each population's deviation from the rest state,
+    and the slowest domains' velocity is ~0.01)."""
+    import marbles_gb300 as M
+    doms = cases.batch_domains(256)
+    states = []
+    for n, nu, v0 in doms:
+        d = M.LBM(inputs.tg_domain(*n, nu=nu, v0=v0), ["lbm.precision=fp64"])
+        d.prepare()
+        states.append(d.initial_state(0))
+        d.close()
+    p, _ = cases.tg_domain(*doms[0][0], nu=doms[0][1], v0=doms[0][2])
+    common = cases.mbg_params_from(p, 1)
+    b = M.Batch(common, [(n, [0.0] * 3, [2 * math.pi] * 3, nu, nu) for n, nu, _ in doms])
+    b.set_state(np.concatenate([f for f, _ in states]), np.concatenate([g for _, g in states]))
+    b.step(2)
+    a = b.get_macro()
+    worst = {"rho": 0.0, "u": 0.0, "T": 0.0}
+    off = 0
+    for (n, nu, v0), (f, g) in zip(doms, states):
+        p, levels = cases.tg_domain(*n, nu=nu, v0=v0)
+        r = M.Context(cases.mbg_params_from(p, 0))
+        r.define_level(0, levels[0], None)
+        r.set_state(0, f, g)
+        r.step(2)
+        R = r.get_macro(0).reshape(19, -1)
+        r.close()
+        vol = int(np.prod(n))
+        A = a[off * 19:(off + vol) * 19].reshape(19, vol)
+        off += vol
+        worst["rho"] = max(worst["rho"], float(np.max(np.abs(A[0] - R[0]) / R[0])))
+        worst["T"] = max(worst["T"], float(np.max(np.abs(A[18] - R[18]) / R[18])))
+        worst["u"] = max(worst["u"], float(np.max(np.abs(A[1:4] - R[1:4])) / np.max(np.abs(R[1:4]))))
+    print("256-domain batch, FP16, 2 steps:", worst)
+    assert worst["rho"] <= 1e-4 and worst["T"] <= 1e-3 and worst["u"] <= 3e-3, worst
