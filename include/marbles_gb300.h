@@ -292,6 +292,45 @@ void mbg_adj_destroy(mbg_adj* a);
 mbg_status mbg_step_box_noalloc(const mbg_params* params, const double* f_in, const double* g_in,
                                 double* f_out, double* g_out, void* cuda_stream);
 
+/* ---- tagging and regrid ------------------------------------------------------
+ * One refinement criterion of tagging.<name>.* (Source/LBM.cpp:302-396):
+ * field 0..18 is a macro component in the order of mbg_get_macro, 19 is
+ * is_fluid (component 0, which the reference's get_field copies for either
+ * id field, Source/LBM.cpp:1536-1546); kind 0 tags every cell whose centre
+ * lies in the box, 1 value_greater, 2 value_less (within the box if
+ * has_box); the criterion applies while start_time <= time <= end_time and
+ * the level is below max_level. */
+#define MBG_MAX_TAGS 8
+typedef struct mbg_tag {
+    int field;
+    int kind;
+    double value;
+    int has_box;
+    double box_lo[3], box_hi[3];
+    double start_time, end_time;
+    int max_level;
+} mbg_tag;
+
+/* Tags (0/1 per valid cell, layout [box][k][j][i]) of level lev at simulated
+ * time `time`, evaluated on the GPU from the level's macro data: in the FP64
+ * form the moments its last collision started from (the reference's
+ * m_macrodata), or those of the stored state when no step has run since the
+ * state was set; in the 16-bit forms the moments of the stored state.
+ * Replaces LBM::ErrorEst (Source/LBM.cpp:1597-1611) with AMReX's
+ * AMRErrorTag. */
+mbg_status mbg_tag_cells(mbg_ctx* ctx, int lev, const mbg_tag* tags, int ntags, double time, uint8_t* out);
+
+/* Replace levels first_lev .. of the hierarchy by nlev levels with new box
+ * arrays (nbox[m] boxes each, lohi concatenated over the levels, flags in the
+ * layout of mbg_define_level concatenated likewise); levels beyond them are
+ * dropped and their device memory freed.  Each new level's cells keep the
+ * old level's values where an old box held them and are interpolated from
+ * the coarser level (conservative linear, on the GPU) elsewhere; solid cells
+ * start at 0.  Replaces LBM::RemakeLevel / MakeNewLevelFromCoarse /
+ * ClearLevel (Source/LBM.cpp:1088-1140, 1302-1379). */
+mbg_status mbg_regrid(mbg_ctx* ctx, int first_lev, int nlev, const int* nbox, const int* lohi,
+                      const uint8_t* flags);
+
 /* ---- embedded-boundary geometry -------------------------------------------
  * eb2.geom_type and its keys (Source/EB.cpp:5-38, Source/Geometry.cpp:5-200):
  * the AMReX built-in sphere, box, cylinder and plane and the reference's own
@@ -407,6 +446,16 @@ mbg_status mbg_lbm_write_plotfile(mbg_lbm* h, const char* name);
  * LBM::write_checkpoint_file / read_checkpoint_file
  * (Source/LBM.cpp:1692-1916). */
 mbg_status mbg_lbm_write_checkpoint(mbg_lbm* h, const char* name);
+
+/* Regrid now: tag every level below amr.max_level on the GPU with the
+ * tagging.* criteria (mbg_tag_cells), rebuild the fine grids from the tags
+ * (buffered by amr.n_error_buf, clustered on amr.blocking_factor blocks,
+ * chopped by amr.max_grid_size, nested), and remake the levels whose grids
+ * changed (mbg_regrid).  mbg_lbm_evolve does this before every coarse step
+ * whose count is a positive multiple of amr.regrid_int, as time_step(0)
+ * does (Source/LBM.cpp:456-479); finer levels' own regrid points inside a
+ * coarse step are not taken. */
+mbg_status mbg_lbm_regrid(mbg_lbm* h);
 
 /* Coarse steps taken and the simulated time of the driver. */
 mbg_status mbg_lbm_step_time(const mbg_lbm* h, int* step, double* time);

@@ -26,7 +26,8 @@ EXPORTS = [
     "mbg_stream", "mbg_set_timing", "mbg_timing_count", "mbg_timing", "mbg_step_box_noalloc",
     "mbg_lbm_create", "mbg_lbm_prepare", "mbg_lbm_initial_state", "mbg_lbm_init", "mbg_lbm_evolve", "mbg_lbm_context", "mbg_lbm_num_levels",
     "mbg_lbm_level_boxes", "mbg_lbm_level_flags", "mbg_lbm_write_plotfile", "mbg_lbm_last_error",
-    "mbg_lbm_destroy", "mbg_lbm_write_checkpoint", "mbg_lbm_step_time",
+    "mbg_lbm_destroy", "mbg_lbm_write_checkpoint", "mbg_lbm_step_time", "mbg_tag_cells", "mbg_regrid", "mbg_lbm_regrid",
+    "mbg_geometry_flags",
     "mbg_get_derived", "mbg_conserved", "mbg_autotune", "mbg_tuning",
     "mbg_write_plotfile", "mbg_write_multifab", "mbg_read_multifab",
     "mbg_batch_create", "mbg_batch_cells", "mbg_batch_set_state", "mbg_batch_get_state", "mbg_batch_get_macro",
@@ -62,6 +63,32 @@ class MbgParams(C.Structure):
     ]
 
 
+class MbgTag(C.Structure):
+    """mirror of mbg_tag (one refinement criterion)"""
+    _fields_ = [("field", C.c_int), ("kind", C.c_int), ("value", C.c_double), ("has_box", C.c_int),
+                ("box_lo", C.c_double * 3), ("box_hi", C.c_double * 3), ("start_time", C.c_double),
+                ("end_time", C.c_double), ("max_level", C.c_int)]
+
+
+# macro field names of mbg_get_macro (Source/Constants.H order) and is_fluid
+FIELDS = ["rho", "vel_x", "vel_y", "vel_z", "vel_mag", "two_rho_e", "QCorrX", "QCorrY", "QCorrZ", "pxx", "pyy",
+          "pzz", "pxy", "pxz", "pyz", "qx", "qy", "qz", "temperature", "is_fluid"]
+
+
+def make_tag(field="rho", kind="greater", value=0.0, box=None, start_time=-1.0e300, end_time=1.0e300,
+             max_level=1000):
+    t = MbgTag()
+    t.field = FIELDS.index(field) if isinstance(field, str) else field
+    t.kind = {"box": 0, "greater": 1, "less": 2}[kind]
+    t.value = value
+    t.has_box = 1 if box is not None else 0
+    if box is not None:
+        t.box_lo[:] = list(box[0])
+        t.box_hi[:] = list(box[1])
+    t.start_time, t.end_time, t.max_level = start_time, end_time, max_level
+    return t
+
+
 class MbgDomain(C.Structure):
     """mirror of mbg_domain (one domain of a batch)"""
     _fields_ = [("n_cell", C.c_int * 3), ("prob_lo", C.c_double * 3), ("prob_hi", C.c_double * 3),
@@ -89,6 +116,9 @@ def lib():
         L.mbg_set_state.argtypes = [vp, C.c_int, dp, dp]
         L.mbg_get_state.argtypes = [vp, C.c_int, dp, dp]
         L.mbg_get_macro.argtypes = [vp, C.c_int, dp]
+        L.mbg_tag_cells.argtypes = [vp, C.c_int, C.POINTER(MbgTag), C.c_int, C.c_double, C.POINTER(C.c_uint8)]
+        L.mbg_regrid.argtypes = [vp, C.c_int, C.c_int, ip, ip, C.POINTER(C.c_uint8)]
+        L.mbg_lbm_regrid.argtypes = [vp]
         L.mbg_get_derived.argtypes = [vp, C.c_int, dp]
         L.mbg_write_plotfile.argtypes = [C.c_char_p, C.c_int, ip, ip, ip, dp, dp, C.c_int,
                                          C.POINTER(C.c_char_p), C.POINTER(dp), C.c_double, ip]
@@ -247,6 +277,32 @@ class Context:
         m = np.empty(self.ncells(lev) * 7)
         self._check(self.L.mbg_get_derived(self.h, lev, _dp(m)), "mbg_get_derived")
         return m
+
+    def tag_cells(self, lev, tags, time):
+        """ErrorEst tags (0/1 per valid cell of level lev, [box][cell])."""
+        arr = (MbgTag * len(tags))(*tags)
+        out = np.zeros(self.ncells(lev), dtype=np.uint8)
+        self._check(self.L.mbg_tag_cells(self.h, lev, arr, len(tags), time,
+                                         out.ctypes.data_as(C.POINTER(C.c_uint8))), "mbg_tag_cells")
+        return out
+
+    def regrid(self, first_lev, levels, flags=None):
+        """Replace levels first_lev.. by the box arrays `levels` (flags per
+        level in the layout of define_level, None: all fluid)."""
+        nbox = np.array([len(b) for b in levels] or [0], dtype=np.int32)
+        parts = [np.asarray(b, dtype=np.int32).reshape(-1) for b in levels]
+        lohi = np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros(6, dtype=np.int32))
+        if flags is None:
+            flags = [np.ones(int(np.prod(np.asarray(b)[:, 3:] - np.asarray(b)[:, :3] + 7, axis=1).sum()),
+                             dtype=np.uint8) for b in levels]
+        fparts = [np.asarray(f, dtype=np.uint8) for f in flags]
+        fl = np.ascontiguousarray(np.concatenate(fparts) if fparts else np.zeros(1, dtype=np.uint8))
+        ipt = C.POINTER(C.c_int)
+        self._check(self.L.mbg_regrid(self.h, first_lev, len(levels), nbox.ctypes.data_as(ipt),
+                                      lohi.ctypes.data_as(ipt), fl.ctypes.data_as(C.POINTER(C.c_uint8))),
+                    "mbg_regrid")
+        if getattr(self, "boxes", None) is not None:
+            self.boxes = self.boxes[:first_lev] + [np.asarray(b) for b in levels]
 
     def step(self, n=1):
         self._check(self.L.mbg_step(self.h, n), "mbg_step")
@@ -527,6 +583,12 @@ class LBM:
 
     def write_plotfile(self, name):
         self._check(self.L.mbg_lbm_write_plotfile(self.h, name.encode()), "mbg_lbm_write_plotfile")
+
+    def regrid(self):
+        """Tag on the GPU, rebuild the fine grids, remake the changed levels."""
+        self._check(self.L.mbg_lbm_regrid(self.h), "mbg_lbm_regrid")
+        if self.ctx is not None:
+            self.ctx.boxes = [self.boxes(l) for l in range(self.num_levels())]
 
     def write_checkpoint(self, name):
         self._check(self.L.mbg_lbm_write_checkpoint(self.h, name.encode()), "mbg_lbm_write_checkpoint")

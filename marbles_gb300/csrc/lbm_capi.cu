@@ -128,6 +128,14 @@ mbg_status mbg_lbm_step_time(const mbg_lbm* h, int* step, double* time)
     return MBG_OK;
 }
 
+mbg_status mbg_lbm_regrid(mbg_lbm* h)
+{
+    if (!h) return MBG_EINVAL;
+    mbg_status st = h->lbm.regrid();
+    if (st != MBG_OK) h->err = h->lbm.err;
+    return st;
+}
+
 const char* mbg_lbm_last_error(const mbg_lbm* h) { return h ? h->err.c_str() : g_lbm_err.c_str(); }
 
 void mbg_lbm_destroy(mbg_lbm* h) { delete h; }

@@ -361,6 +361,8 @@ bool LBM::configure(const Inputs& in, std::string& e)
             for (int d = 0; d < 3; ++d) { t.box_lo[d] = blo[d]; t.box_hi[d] = bhi[d]; }
         }
         in.query(pre + "max_level", t.max_level);
+        in.query(pre + "start_time", t.start_time);
+        in.query(pre + "end_time", t.end_time);
         double v;
         if (in.query(pre + "value_greater", v)) { t.kind = 1; t.value = v; }
         else if (in.query(pre + "value_less", v)) { t.kind = 2; t.value = v; }
@@ -373,8 +375,18 @@ bool LBM::configure(const Inputs& in, std::string& e)
         }
         if (t.kind) {
             in.query(pre + "field_name", t.field);
-            if (t.field != "is_fluid") {
-                e = "tagging: only the is_fluid field can be tagged with static grids";
+            // the macro fields and the id fields (get_field copies is_fluid
+            // component 0 for either id name, Source/LBM.cpp:1536-1546)
+            static const char* names[19] = {"rho", "vel_x", "vel_y", "vel_z", "vel_mag", "two_rho_e", "QCorrX",
+                                            "QCorrY", "QCorrZ", "pxx", "pyy", "pzz", "pxy", "pxz", "pyz",
+                                            "qx", "qy", "qz", "temperature"};
+            t.field_index = -1;
+            for (int k = 0; k < 19; ++k)
+                if (t.field == names[k]) t.field_index = k;
+            if (t.field == "is_fluid" || t.field == "eb_boundary") t.field_index = 19;
+            if (t.field_index < 0) {
+                e = "LBM::read_tagging_parameters(): unknown variable field for tagging criteria " + name +
+                    " (the macro fields, is_fluid, eb_boundary)";
                 return false;
             }
         }
@@ -537,7 +549,7 @@ void LBM::make_flags(int lev)
 // static grids: level 0 chopped by max_grid_size; finer levels from the
 // tagging criteria, buffered, clustered on blocking-factor blocks, chopped
 // ---------------------------------------------------------------------------
-bool LBM::make_grids(std::string& e)
+bool LBM::make_grids(std::string& e, const std::vector<std::vector<uint8_t>>* dense)
 {
     Box dom;
     for (int d = 0; d < 3; ++d) { dom.lo[d] = 0; dom.hi[d] = cfg_.n_cell[d] - 1; }
@@ -561,8 +573,15 @@ bool LBM::make_grids(std::string& e)
             for (int j = 0; j < n[1]; ++j)
                 for (int i = 0; i < n[0]; ++i) {
                     bool t = false;
+                    if (dense) {
+                        // tags evaluated on the GPU (mbg_tag_cells) where the level exists
+                        const auto& dl = (*dense)[lev];
+                        t = !dl.empty() && dl[((size_t)k * n[1] + j) * n[0] + i];
+                    }
                     for (const auto& tg : cfg_.tags) {
-                        if (lev >= tg.max_level) continue;
+                        if (dense) break;
+                        if (lev >= tg.max_level || !(0.0 >= tg.start_time && 0.0 <= tg.end_time)) continue;
+                        if (tg.kind != 0 && tg.field_index != 19) continue;   // state fields: tagged on the GPU
                         bool inbox = true;
                         if (tg.has_box) {
                             const double c[3] = {cfg_.prob_lo[0] + (i + 0.5) * dx[0], cfg_.prob_lo[1] + (j + 0.5) * dx[1],
@@ -815,11 +834,17 @@ mbg_status LBM::prepare()
     return MBG_OK;
 }
 
-mbg_status LBM::init_data()
+bool LBM::has_field_tags() const
 {
-    mbg_status st0 = prepare();
-    if (st0 != MBG_OK) return st0;
-    mbg_params p;
+    for (const auto& t : cfg_.tags)
+        if (t.kind != 0 && t.field_index != 19) return true;
+    return false;
+}
+
+// the context, the levels with their GPU flags and (no restart) the IC
+mbg_status LBM::build_context()
+{
+    mbg_params& p = params_;
     std::memset(&p, 0, sizeof(p));
     for (int d = 0; d < 3; ++d) {
         p.n_cell[d] = cfg_.n_cell[d];
@@ -841,6 +866,7 @@ mbg_status LBM::init_data()
     p.vbc_u_ref = vbc_.u_ref; p.vbc_initial_density = vbc_.initial_density;
     p.vbc_initial_temperature = vbc_.initial_temperature; p.vbc_adiabatic_exponent = vbc_.adiabatic_exponent;
     p.vbc_m_bar = vbc_.m_bar;
+    if (ctx_) { mbg_destroy(ctx_); ctx_ = nullptr; }
     mbg_status st = mbg_create(&p, nullptr, &ctx_);
     if (st != MBG_OK) { err = mbg_last_error(nullptr); return st; }
     for (size_t lev = 0; lev < grids_.size(); ++lev) {
@@ -848,10 +874,8 @@ mbg_status LBM::init_data()
         for (const Box& b : grids_[lev])
             for (int x : {b.lo[0], b.lo[1], b.lo[2], b.hi[0], b.hi[1], b.hi[2]}) lohi.push_back(x);
         // the level's is_fluid flags from the geometry, on the GPU (the grids
-        // above were tagged from the same implicit functions on the host)
-        st = mbg_geometry_flags(&cfg_.geom, &p, (int)lev, (int)grids_[lev].size(), lohi.data(), flags_[lev].data(),
-                                mbg_stream(ctx_));
-        if (st != MBG_OK) { err = mbg_last_error(nullptr); return st; }
+        // were tagged from the same implicit functions on the host)
+        if ((st = level_flags_gpu((int)lev, flags_[lev])) != MBG_OK) return st;
         st = mbg_define_level(ctx_, (int)lev, (int)grids_[lev].size(), lohi.data(), flags_[lev].data());
         if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
         if (!cfg_.restart.empty()) continue;
@@ -859,6 +883,120 @@ mbg_status LBM::init_data()
         initial_state((int)lev, f, g);
         st = mbg_set_state(ctx_, (int)lev, f.data(), g.data());
         if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
+    }
+    return MBG_OK;
+}
+
+mbg_status LBM::level_flags_gpu(int lev, std::vector<uint8_t>& out)
+{
+    std::vector<int> lohi;
+    long long n = 0;
+    for (const Box& b : grids_[lev]) {
+        for (int x : {b.lo[0], b.lo[1], b.lo[2], b.hi[0], b.hi[1], b.hi[2]}) lohi.push_back(x);
+        n += (long long)(b.n(0) + 6) * (b.n(1) + 6) * (b.n(2) + 6);
+    }
+    out.resize((size_t)n);
+    mbg_status st = mbg_geometry_flags(&cfg_.geom, &params_, lev, (int)grids_[lev].size(), lohi.data(), out.data(),
+                                       ctx_ ? mbg_stream(ctx_) : nullptr);
+    if (st != MBG_OK) err = mbg_last_error(nullptr);
+    return st;
+}
+
+mbg_status LBM::gpu_tags(std::vector<std::vector<uint8_t>>& dense)
+{
+    const int nlev = (int)grids_.size();
+    dense.assign(cfg_.max_level, {});
+    std::vector<mbg_tag> tags;
+    for (const auto& t : cfg_.tags) {
+        mbg_tag g{};
+        g.field = t.field_index;
+        g.kind = t.kind;
+        g.value = t.value;
+        g.has_box = t.has_box ? 1 : 0;
+        for (int d = 0; d < 3; ++d) { g.box_lo[d] = t.box_lo[d]; g.box_hi[d] = t.box_hi[d]; }
+        g.start_time = t.start_time;
+        g.end_time = t.end_time;
+        g.max_level = t.max_level;
+        tags.push_back(g);
+    }
+    if ((int)tags.size() > MBG_MAX_TAGS) { err = "tagging: at most 8 refinement indicators"; return MBG_EINVAL; }
+    for (int lev = 0; lev < std::min(nlev, cfg_.max_level); ++lev) {
+        long long ncell = 0;
+        for (const Box& b : grids_[lev]) ncell += b.vol();
+        std::vector<uint8_t> t((size_t)ncell);
+        mbg_status st = mbg_tag_cells(ctx_, lev, tags.data(), (int)tags.size(), time_, t.data());
+        if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
+        const int n[3] = {cfg_.n_cell[0] << lev, cfg_.n_cell[1] << lev, cfg_.n_cell[2] << lev};
+        auto& D = dense[lev];
+        D.assign((size_t)n[0] * n[1] * n[2], 0);
+        long long off = 0;
+        for (const Box& b : grids_[lev])
+            for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+                for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+                    for (int i = b.lo[0]; i <= b.hi[0]; ++i, ++off)
+                        D[((size_t)k * n[1] + j) * n[0] + i] = t[(size_t)off];
+    }
+    return MBG_OK;
+}
+
+static bool same_grids(const std::vector<std::vector<Box>>& a, const std::vector<std::vector<Box>>& b)
+{
+    if (a.size() != b.size()) return false;
+    for (size_t l = 0; l < a.size(); ++l) {
+        if (a[l].size() != b[l].size()) return false;
+        for (size_t n = 0; n < a[l].size(); ++n)
+            for (int d = 0; d < 3; ++d)
+                if (a[l][n].lo[d] != b[l][n].lo[d] || a[l][n].hi[d] != b[l][n].hi[d]) return false;
+    }
+    return true;
+}
+
+mbg_status LBM::regrid()
+{
+    if (!ctx_) { err = "regrid: the driver is not initialised"; return MBG_ESTATE; }
+    if (cfg_.max_level <= 0) return MBG_OK;
+    std::vector<std::vector<uint8_t>> dense;
+    mbg_status st = gpu_tags(dense);
+    if (st != MBG_OK) return st;
+    const std::vector<std::vector<Box>> old = grids_;
+    if (!make_grids(err, &dense)) return MBG_EINVAL;
+    if (same_grids(old, grids_)) return MBG_OK;
+    const int nlev = (int)grids_.size();
+    flags_.resize(nlev);
+    std::vector<int> nbox, lohi;
+    std::vector<uint8_t> fl;
+    for (int lev = 1; lev < nlev; ++lev) {
+        if ((st = level_flags_gpu(lev, flags_[lev])) != MBG_OK) return st;
+        nbox.push_back((int)grids_[lev].size());
+        for (const Box& b : grids_[lev])
+            for (int x : {b.lo[0], b.lo[1], b.lo[2], b.hi[0], b.hi[1], b.hi[2]}) lohi.push_back(x);
+        fl.insert(fl.end(), flags_[lev].begin(), flags_[lev].end());
+    }
+    st = mbg_regrid(ctx_, 1, nlev - 1, nbox.data(), lohi.data(), fl.data());
+    if (st != MBG_OK) err = mbg_last_error(ctx_);
+    return st;
+}
+
+mbg_status LBM::init_data()
+{
+    mbg_status st = prepare();
+    if (st != MBG_OK) return st;
+    if ((st = build_context()) != MBG_OK) return st;
+    if (cfg_.restart.empty() && has_field_tags()) {
+        // InitFromScratch tags each level on its initial data
+        // (MakeNewLevelFromScratch, then ErrorEst): tag the initial state on
+        // the GPU, rebuild the grids and start again from the IC until the
+        // grids stop changing (at most max_level rounds)
+        for (int it = 0; it < cfg_.max_level; ++it) {
+            std::vector<std::vector<uint8_t>> dense;
+            if ((st = gpu_tags(dense)) != MBG_OK) return st;
+            const std::vector<std::vector<Box>> old = grids_;
+            if (!make_grids(err, &dense)) return MBG_EINVAL;
+            if (same_grids(old, grids_)) break;
+            flags_.assign(grids_.size(), {});
+            for (size_t lev = 0; lev < grids_.size(); ++lev) make_flags((int)lev);
+            if ((st = build_context()) != MBG_OK) return st;
+        }
     }
     if (!cfg_.restart.empty()) {
         // LBM::init_data's restart branch (Source/LBM.cpp:177-182)
@@ -878,6 +1016,7 @@ mbg_status LBM::init_data()
         }
         if (cfg_.compute_forces) write_forces(true);
     }
+    last_regrid_step_ = step_;
     if (cfg_.plot_int > 0) {
         st = write_plot_file(numbered(cfg_.plot_file));
         if (st != MBG_OK) return st;
@@ -908,6 +1047,14 @@ mbg_status LBM::evolve(int nsteps)
     const bool to_end = nsteps <= 0;
     const int last = to_end ? cfg_.max_step : step_ + nsteps;
     while (step_ < last && time_ < cfg_.stop_time) {
+        // the regrid branch of time_step(0) (Source/LBM.cpp:456-479): before
+        // a coarse step whose count is a multiple of amr.regrid_int
+        if (cfg_.regrid_int > 0 && cfg_.max_level > 0 && step_ > last_regrid_step_ &&
+            step_ % cfg_.regrid_int == 0) {
+            mbg_status sr = regrid();
+            if (sr != MBG_OK) return sr;
+            last_regrid_step_ = step_;
+        }
         mbg_status st = mbg_step(ctx_, 1);
         if (st != MBG_OK) { err = mbg_last_error(ctx_); return st; }
         ++step_;

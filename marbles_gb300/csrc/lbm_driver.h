@@ -80,9 +80,11 @@ struct Config {
         bool has_box = false;
         double box_lo[3], box_hi[3];
         std::string field;
+        int field_index = 19;  // macro component 0..18 (mbg_get_macro order) or 19 = is_fluid
         int kind = 0;  // 0 box only, 1 value_greater, 2 value_less
         double value = 0.0;
         int max_level = 1000;
+        double start_time = -1.0e300, end_time = 1.0e300;
     };
     std::vector<Tag> tags;
     // the form of the populations
@@ -121,6 +123,9 @@ public:
     mbg_status evolve(int nsteps);      // nsteps <= 0: run to max_step / stop_time
     mbg_status write_plot_file(const std::string& name);
     mbg_status write_checkpoint(const std::string& name);
+    // ErrorEst on the GPU, new grids from the tags, RemakeLevel of levels >= 1
+    // (Source/LBM.cpp:452-521 regrid branch); no-op when the grids do not change
+    mbg_status regrid();
     mbg_ctx* context() { return ctx_; }
     const Config& config() const { return cfg_; }
     const std::vector<std::vector<Box>>& grids() const { return grids_; }
@@ -144,7 +149,16 @@ private:
     int step_ = 0;
     double time_ = 0.0;
     int last_plot_step_ = -1;
+    int last_regrid_step_ = 0;
     bool prepared_ = false;
+    mbg_params params_{};
+
+    mbg_status build_context();
+    bool has_field_tags() const;
+    // per level below max_level that exists: the tags of every cell of the
+    // level's index space (x fastest), 0 outside the level's boxes
+    mbg_status gpu_tags(std::vector<std::vector<uint8_t>>& dense);
+    mbg_status level_flags_gpu(int lev, std::vector<uint8_t>& out);
 
     mbg_status read_checkpoint();
     std::string numbered(const std::string& root) const;
@@ -152,7 +166,7 @@ private:
     void level_geometry(int lev, double dx[3]) const;
     bool covered_cell(int lev, int i, int j, int k) const;
     void make_flags(int lev);
-    bool make_grids(std::string& e);
+    bool make_grids(std::string& e, const std::vector<std::vector<uint8_t>>* dense = nullptr);
     void ic_state(int lev, int i, int j, int k, double& rho, double vel[3], double& t, double& Rg,
                   double& gamma) const;
     void write_forces(bool init);

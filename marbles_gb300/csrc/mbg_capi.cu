@@ -75,6 +75,11 @@ struct Level {
     int cur = 0;
     double dt = 1.0;
     double dx[3], idx[3];
+    // the FP64 macro scratch holds the moments the level's last collision
+    // started from (false after a state upload or a remake)
+    bool md_valid = false;
+    // the level's entries of mbg_ctx::allocs (freed when a regrid drops it)
+    size_t alloc_begin = 0, alloc_end = 0;
     LevelPlan plan;
     LowpLevel lowp;   // 16-bit storage form buffers (mbg_lowp.cu)
 };
@@ -463,6 +468,7 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     if (lev != (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_define_level: levels must be defined in order 0, 1, ...");
     if (nbox <= 0 || !lohi) return fail(ctx, MBG_EINVAL, "mbg_define_level: need at least one box");
     const mbg_params& p = ctx->p;
+    const size_t alloc_begin = ctx->allocs.size();
     Level L;
     const int r = 1 << lev;
     for (int d = 0; d < 3; ++d) {
@@ -755,6 +761,8 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     MBG_CUDA(cudaStreamSynchronize(ctx->s));
     ctx->lv.push_back(std::move(L));
     Level& LL = ctx->lv.back();
+    LL.alloc_begin = alloc_begin;
+    LL.alloc_end = ctx->allocs.size();
     refresh_plan(ctx, LL);
     if (p.precision != MBG_FP64) {
         LevelHost host;
@@ -779,6 +787,7 @@ mbg_status mbg_set_state(mbg_ctx* ctx, int lev, const double* f, const double* g
     if (!ctx) return MBG_EINVAL;
     if (lev < 0 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_set_state: level not defined");
     Level& L = ctx->lv[lev];
+    L.md_valid = false;
     if (ctx->p.precision != MBG_FP64) {
         mbg_status s2 = lowp_set_state(L.lowp, L.plan, L.hbox, f, g, ctx->s, ctx->err);
         ctx->launches += 2;
@@ -916,6 +925,7 @@ static mbg_status advance(mbg_ctx* ctx, int lev)
     ctx->launches += 2 * fp64_step_launches(L.plan);
     MBG_CUDA(cudaGetLastError());
     L.cur = Bf;
+    L.md_valid = true;
     return MBG_OK;
 }
 
@@ -1139,6 +1149,164 @@ mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3])
     MBG_CUDA(cudaGetLastError());
     MBG_CUDA(cudaMemcpyAsync(out, ctx->d_red, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
     MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+// ---- tagging and regrid ------------------------------------------------------
+mbg_status mbg_tag_cells(mbg_ctx* ctx, int lev, const mbg_tag* tags, int ntags, double time, uint8_t* out)
+{
+    if (!ctx || !out || ntags < 0 || (ntags > 0 && !tags)) return MBG_EINVAL;
+    if (lev < 0 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_ESTATE, "mbg_tag_cells: level not defined");
+    if (ntags > MBG_MAX_TAGS) return fail(ctx, MBG_EINVAL, "mbg_tag_cells: too many criteria");
+    TagSet ts;
+    ts.n = ntags;
+    for (int c = 0; c < ntags; ++c) {
+        const mbg_tag& t = tags[c];
+        if (t.field < 0 || t.field > 19 || t.kind < 0 || t.kind > 2)
+            return fail(ctx, MBG_EINVAL, "mbg_tag_cells: field must be 0..19 and kind 0..2");
+        ts.t[c] = t;
+    }
+    Level& L = ctx->lv[lev];
+    const double *f, *g, *fg, *gg;
+    mbg_status st = fp64_state(ctx, L, true, &f, &g, &fg, &gg);
+    if (st != MBG_OK) return st;
+    const size_t need = (size_t)L.N * 19;
+    if (ctx->out19_n < need) {
+        if ((st = dalloc(ctx, &ctx->d_out19, need)) != MBG_OK) return st;
+        ctx->out19_n = need;
+    }
+    const bool md = ctx->p.precision == MBG_FP64 && L.md_valid;
+    double plo[3];
+    for (int d = 0; d < 3; ++d) plo[d] = ctx->p.prob_lo[d];
+    launch_tags(L.plan, phys64(ctx, L), md ? L.md : nullptr, f, g, ts, time, lev, plo, L.dx,
+                (uint8_t*)ctx->d_out19, ctx->s);
+    ctx->launches++;
+    MBG_CUDA(cudaGetLastError());
+    MBG_CUDA(cudaMemcpyAsync(out, ctx->d_out19, (size_t)L.N, cudaMemcpyDeviceToHost, ctx->s));
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+// frees the device memory of levels first.. and forgets them; the coarser
+// level loses its coalescence lists and override flags
+static mbg_status drop_levels(mbg_ctx* ctx, int first)
+{
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    for (int l = (int)ctx->lv.size() - 1; l >= first; --l) {
+        Level& L = ctx->lv[l];
+        if (L.lowp.impl) lowp_release(L.lowp);
+        for (size_t i = L.alloc_begin; i < L.alloc_end && i < ctx->allocs.size(); ++i) {
+            cudaFree(ctx->allocs[i]);
+            ctx->allocs[i] = nullptr;
+        }
+    }
+    ctx->lv.resize(first);
+    Level& C = ctx->lv[first - 1];
+    C.d_coal1 = C.d_coal0 = nullptr;
+    C.ncoal1 = C.ncoal0 = 0;
+    for (auto& v : C.hflags) v = (uint8_t)(v & ~(FL_OVR | FL_COV));
+    MBG_CUDA(cudaMemcpyAsync(C.d_flags, C.hflags.data(), C.hflags.size(), cudaMemcpyHostToDevice, ctx->s));
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+mbg_status mbg_regrid(mbg_ctx* ctx, int first_lev, int nlev, const int* nbox, const int* lohi, const uint8_t* flags)
+{
+    if (!ctx || nlev < 0 || (nlev > 0 && (!nbox || !lohi || !flags))) return MBG_EINVAL;
+    if (first_lev < 1 || first_lev > (int)ctx->lv.size())
+        return fail(ctx, MBG_EINVAL, "mbg_regrid: first_lev must be 1 .. number of levels");
+    drop_graph(ctx);
+    // the old fine levels' state on the host, with their boxes
+    struct Old { std::vector<HBox> boxes; std::vector<long long> off; std::vector<double> f, g; };
+    std::vector<Old> old;
+    for (int l = first_lev; l < (int)ctx->lv.size(); ++l) {
+        Old o;
+        o.boxes = ctx->lv[l].boxes;
+        long long n = 0;
+        for (const HBox& b : o.boxes) { o.off.push_back(n); n += b.vol(); }
+        o.f.resize((size_t)n * NQ);
+        o.g.resize((size_t)n * NQ);
+        mbg_status st = mbg_get_state(ctx, l, o.f.data(), o.g.data());
+        if (st != MBG_OK) return st;
+        old.push_back(std::move(o));
+    }
+    mbg_status st = drop_levels(ctx, first_lev);
+    if (st != MBG_OK) return st;
+    long long boff = 0, foff = 0;
+    for (int m = 0; m < nlev; ++m) {
+        const int lev = first_lev + m;
+        st = mbg_define_level(ctx, lev, nbox[m], lohi + 6 * boff, flags + foff);
+        if (st != MBG_OK) return st;
+        Level& F = ctx->lv[lev];
+        Level& C = ctx->lv[lev - 1];
+        // the interpolation stencil of every new cell must lie in the coarse level
+        for (const HBox& b : F.boxes)
+            for (int z = b.lo[2] / 2 - 1; z <= b.hi[2] / 2 + 1; ++z)
+                for (int y = b.lo[1] / 2 - 1; y <= b.hi[1] / 2 + 1; ++y)
+                    for (int x = b.lo[0] / 2 - 1; x <= b.hi[0] / 2 + 1; ++x) {
+                        int c[3] = {x, y, z};
+                        if (!wrap_host(C, ctx->p.is_periodic, c) || owner_host(C, c) < 0)
+                            return fail(ctx, MBG_EINVAL, "mbg_regrid: level " + std::to_string(lev) +
+                                                             " is not properly nested in level " +
+                                                             std::to_string(lev - 1));
+                    }
+        // coarse-to-fine interpolation of every new cell on the GPU
+        const double *cf, *cg, *cfg, *cgg;
+        if ((st = fp64_state(ctx, C, true, &cf, &cg, &cfg, &cgg)) != MBG_OK) return st;
+        double *d_if = nullptr, *d_ig = nullptr;
+        cudaError_t e = cudaMalloc(&d_if, (size_t)F.N * NQ * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&d_ig, (size_t)F.N * NQ * sizeof(double));
+        std::vector<double> nf((size_t)F.N * NQ), ng((size_t)F.N * NQ);
+        if (e == cudaSuccess) {
+            launch_interp_level(F.plan, C.plan, cf, d_if, ctx->s);
+            launch_interp_level(F.plan, C.plan, cg, d_ig, ctx->s);
+            ctx->launches += 2;
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(nf.data(), d_if, nf.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ng.data(), d_ig, ng.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->s);
+        cudaFree(d_if);
+        cudaFree(d_ig);
+        if (e != cudaSuccess) return fail(ctx, MBG_ECUDA, std::string("mbg_regrid: ") + cudaGetErrorString(e));
+        // cells an old box held keep their values; solid cells start at 0
+        // (fill_f_inside_eb, Source/LBM.cpp:1278-1298)
+        const Old* O = m < (int)old.size() ? &old[m] : nullptr;
+        long long off = 0, goff = 0;
+        for (size_t n = 0; n < F.boxes.size(); ++n) {
+            const HBox& b = F.boxes[n];
+            const long long v = b.vol();
+            long long c = 0;
+            for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+                for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+                    for (int i = b.lo[0]; i <= b.hi[0]; ++i, ++c) {
+                        const uint8_t fl = flags[foff + goff + ((long long)(k - b.lo[2] + 3) * (b.n(1) + 6) +
+                                                                (j - b.lo[1] + 3)) * (b.n(0) + 6) + (i - b.lo[0] + 3)];
+                        if (!(fl & FL_FLUID)) {
+                            for (int q = 0; q < NQ; ++q) nf[off * NQ + q * v + c] = ng[off * NQ + q * v + c] = 0.0;
+                            continue;
+                        }
+                        if (!O) continue;
+                        for (size_t ob = 0; ob < O->boxes.size(); ++ob) {
+                            const HBox& B = O->boxes[ob];
+                            if (i < B.lo[0] || i > B.hi[0] || j < B.lo[1] || j > B.hi[1] || k < B.lo[2] || k > B.hi[2])
+                                continue;
+                            const long long ov = B.vol();
+                            const long long oc = ((long long)(k - B.lo[2]) * B.n(1) + (j - B.lo[1])) * B.n(0) + (i - B.lo[0]);
+                            for (int q = 0; q < NQ; ++q) {
+                                nf[off * NQ + q * v + c] = O->f[O->off[ob] * NQ + q * ov + oc];
+                                ng[off * NQ + q * v + c] = O->g[O->off[ob] * NQ + q * ov + oc];
+                            }
+                            break;
+                        }
+                    }
+            off += v;
+            goff += b.gvol();
+        }
+        if ((st = mbg_set_state(ctx, lev, nf.data(), ng.data())) != MBG_OK) return st;
+        boff += nbox[m];
+        foff += goff;
+    }
     return MBG_OK;
 }
 

@@ -186,4 +186,54 @@ void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParam
                                            fcAg, gcAg, fcB, gcB, into_state);
 }
 
+// ---- regrid: every cell of a new fine level from the coarse level ----------
+// (LBM::RemakeLevel / MakeNewLevelFromCoarse through FillPatchTwoLevels /
+// InterpFromCoarseLevel with cell_cons_interp: per fine cell, the coarse
+// parent's value, centred and MC-limited one-sided slopes, one limiter factor
+// per direction over the 27 components, and the value at the child's offset)
+__global__ void k_interp_level(LV F, LV C, const Tile* tiles, const double* c, double* out)
+{
+    int b, x, y, z;
+    long long cl;
+    if (!cell_of_tile(F, tiles, b, x, y, z, cl)) return;
+    const DevBox& B = F.box[b];
+    const int f[3] = {B.lo[0] + x, B.lo[1] + y, B.lo[2] + z};
+    const int p0[3] = {f[0] >> 1, f[1] >> 1, f[2] >> 1};
+    const long long i0 = crse_index(C, p0, 0, 0);
+    long long ip[3], im[3];
+    for (int d = 0; d < 3; ++d) {
+        ip[d] = crse_index(C, p0, d, 1);
+        im[d] = crse_index(C, p0, d, -1);
+    }
+    const long long vol = (long long)B.n[0] * B.n[1] * B.n[2];
+    double* o = out + B.hoff * NQ + cl;
+    if (i0 < 0 || ip[0] < 0 || ip[1] < 0 || ip[2] < 0 || im[0] < 0 || im[1] < 0 || im[2] < 0) {
+        for (int n = 0; n < NQ; ++n) o[n * vol] = __longlong_as_double(0x7FF8000000000000LL);
+        return;   // the host checks nesting first; a NaN marks a stencil outside the coarse level
+    }
+    double alpha[3] = {1.0, 1.0, 1.0};
+    for (int d = 0; d < 3; ++d)
+        for (int n = 0; n < NQ; ++n) {
+            const double u0 = c[n * C.N + i0], up = c[n * C.N + ip[d]], um = c[n * C.N + im[d]];
+            const double cen = 0.5 * (up - um);
+            const double forw = 2.0 * (up - u0);
+            const double back = 2.0 * (u0 - um);
+            const double slp = (forw * back >= 0.0) ? fmin(fabs(forw), fabs(back)) : 0.0;
+            if (cen != 0.0) alpha[d] = fmin(alpha[d], fmin(slp, fabs(cen)) / fabs(cen));
+        }
+    double off[3];
+    for (int d = 0; d < 3; ++d) off[d] = ((f[d] - 2 * p0[d]) + 0.5) / 2.0 - 0.5;
+    for (int n = 0; n < NQ; ++n) {
+        const double u0 = c[n * C.N + i0];
+        double cen[3];
+        for (int d = 0; d < 3; ++d) cen[d] = 0.5 * (c[n * C.N + ip[d]] - c[n * C.N + im[d]]);
+        o[n * vol] = u0 + off[0] * (alpha[0] * cen[0]) + off[1] * (alpha[1] * cen[1]) + off[2] * (alpha[2] * cen[2]);
+    }
+}
+
+void launch_interp_level(const LevelPlan& fine, const LevelPlan& crse, const double* c, double* out, cudaStream_t s)
+{
+    if (fine.ntiles > 0) k_interp_level<<<fine.ntiles, TILE_CELLS, 0, s>>>(fine.view64, crse.view64, fine.tiles, c, out);
+}
+
 }  // namespace mbg

@@ -267,4 +267,81 @@ void launch_derived(const LevelPlan& lp, const Phys64& ph, const double* f, cons
     k_derived<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, ph, lp.tiles, f, g, fg, gg, out7);
 }
 
+// ---- ErrorEst tags (Source/LBM.cpp:1597-1611, AMReX AMRErrorTag) ------------
+struct Geo3 {
+    double plo[3], dx[3];
+};
+
+__global__ void k_tags(LV L, Phys64 ph, const Tile* tiles, const double* md, const double* f, const double* g,
+                       TagSet ts, double time, int lev, Geo3 geo, uint8_t* out)
+{
+    int b, x, y, z;
+    long long c;
+    if (!cell_of_tile(L, tiles, b, x, y, z, c)) return;
+    const DevBox& B = L.box[b];
+    const uint8_t tf = flag_at(L, B, x, y, z);
+    const long long cell = B.voff + c;
+    double m[19];
+    bool have = false;
+    uint8_t t = 0;
+    for (int k = 0; k < ts.n; ++k) {
+        const mbg_tag& tg = ts.t[k];
+        if (!(time >= tg.start_time && time <= tg.end_time) || lev >= tg.max_level) continue;
+        if (tg.has_box) {
+            const int p[3] = {B.lo[0] + x, B.lo[1] + y, B.lo[2] + z};
+            bool in = true;
+            for (int d = 0; d < 3; ++d) {
+                const double xc = geo.plo[d] + (p[d] + 0.5) * geo.dx[d];
+                in &= xc >= tg.box_lo[d] && xc <= tg.box_hi[d];
+            }
+            if (!in) continue;
+        }
+        if (tg.kind == 0) { t = 1; continue; }
+        double v;
+        if (tg.field == 19) {
+            v = (tf & FL_FLUID) ? 1.0 : 0.0;
+        } else {
+            if (!have) {
+                have = true;
+                if (!(tf & FL_FLUID)) {
+                    for (int q = 0; q < 19; ++q) m[q] = 0.0;   // the macro data of solid cells stays 0
+                } else if (md) {
+                    const long long N = L.N;
+                    const double u = md[MD_U * N + cell], vv = md[MD_V * N + cell], w = md[MD_W * N + cell];
+                    const double vals[19] = {md[MD_RHO * N + cell], u, vv, w, sqrt(u * u + vv * vv + w * w),
+                                             md[MD_TRE * N + cell], md[MD_QCX * N + cell], md[MD_QCY * N + cell],
+                                             md[MD_QCZ * N + cell], md[MD_PXX * N + cell], md[MD_PYY * N + cell],
+                                             md[MD_PZZ * N + cell], md[MD_PXY * N + cell], md[MD_PXZ * N + cell],
+                                             md[MD_PYZ * N + cell], md[MD_QX * N + cell], md[MD_QY * N + cell],
+                                             md[MD_QZ * N + cell], md[MD_T * N + cell]};
+                    for (int q = 0; q < 19; ++q) m[q] = vals[q];
+                } else {
+                    MomentAcc<double> acc;
+#define MBG_TG64(q) acc.template add<q>(f[q * L.N + cell], g[q * L.N + cell]);
+                    MBG_UNROLL27(MBG_TG64)
+#undef MBG_TG64
+                    const Macro<double> a = acc.finish(ph.mesh_speed, ph.Rg, ph.cv);
+                    const double vals[19] = {a.rho, a.u, a.v, a.w, sqrt(a.u * a.u + a.v * a.v + a.w * a.w),
+                                             a.two_rho_e, a.qcx, a.qcy, a.qcz, a.pxx, a.pyy, a.pzz, a.pxy, a.pxz,
+                                             a.pyz, a.qx, a.qy, a.qz, a.temp};
+                    for (int q = 0; q < 19; ++q) m[q] = vals[q];
+                }
+            }
+            v = m[tg.field];
+        }
+        if ((tg.kind == 1 && v > tg.value) || (tg.kind == 2 && v < tg.value)) t = 1;
+    }
+    out[B.hoff + c] = t;
+}
+
+void launch_tags(const LevelPlan& lp, const Phys64& ph, const double* md, const double* f, const double* g,
+                 const TagSet& ts, double time, int lev, const double plo[3], const double dx[3], uint8_t* out,
+                 cudaStream_t s)
+{
+    if (lp.ntiles == 0) return;
+    Geo3 geo;
+    for (int d = 0; d < 3; ++d) { geo.plo[d] = plo[d]; geo.dx[d] = dx[d]; }
+    k_tags<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, ph, lp.tiles, md, f, g, ts, time, lev, geo, out);
+}
+
 }  // namespace mbg

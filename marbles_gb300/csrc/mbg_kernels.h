@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/marbles_gb300.h"
 #include "mbg_level.cuh"
 
 namespace mbg {
@@ -106,6 +107,22 @@ void launch_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, co
 void launch_collide(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
                     const double* fAg, const double* gAg, double* fB, double* gB, const double* md,
                     const double* gqc, cudaStream_t s);
+// the refinement criteria of one mbg_tag_cells call
+struct TagSet {
+    int n = 0;
+    mbg_tag t[MBG_MAX_TAGS];
+};
+// ErrorEst tags of a level's valid cells into out ([box][cell], 0/1): field
+// values from md (the FP64 macro scratch of the last collision) when given,
+// else from the moments of the stored state f, g (FP64 layout)
+void launch_tags(const LevelPlan& lp, const Phys64& ph, const double* md, const double* f, const double* g,
+                 const TagSet& ts, double time, int lev, const double plo[3], const double dx[3], uint8_t* out,
+                 cudaStream_t s);
+// conservative linear interpolation (cell_cons_interp) of every valid cell
+// of a fine level from the coarse level's stored values c (FP64 layout of
+// the coarse plan), one lattice, into out in host layout [box][q][cell]
+void launch_interp_level(const LevelPlan& fine, const LevelPlan& crse, const double* c, double* out,
+                         cudaStream_t s);
 // kernel launches of one launch_moments or launch_collide call
 int fp64_step_launches(const LevelPlan& lp);
 void launch_ghost_stream(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA,

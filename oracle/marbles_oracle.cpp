@@ -271,6 +271,21 @@ typedef struct orc_params {
 
 namespace orc {
 
+extern "C" {
+// one refinement criterion of tagging.<name>.* (field: macro component
+// 0..18 in Source/Constants.H order, 19 = is_fluid; kind 0 box only,
+// 1 value_greater, 2 value_less)
+struct orc_tag {
+    int field;
+    int kind;
+    double value;
+    int has_box;
+    double box_lo[3], box_hi[3];
+    double start_time, end_time;
+    int max_level;
+};
+}
+
 struct Level {
     IBox domain;
     double dx[3], idx[3], plo[3];
@@ -1283,6 +1298,103 @@ struct Sim {
         }
     }
 
+    // ---- ErrorEst (LBM.cpp:1597-1611, AMReX AMRErrorTag) ---------------------
+    // Tags of level lev's valid cells from the level's macro data (the
+    // moments its last collision started from, or those of the state at
+    // initialisation / remake): a criterion applies while start_time <= time
+    // <= end_time and lev < max_level; with a box only cells whose centre lies
+    // in the box (bounds included) are tagged; GREATER / LESS compare the
+    // field with the value.  Field 19 is is_fluid component 0 (get_field
+    // copies that component for either id field name, LBM.cpp:1536-1546).
+    void tag_level(int lev, const orc_tag* tags, int ntags, double time, uint8_t* out) const
+    {
+        const Level& L = lv[lev];
+        size_t off = 0;
+        for (size_t n = 0; n < L.ba.size(); ++n) {
+            const IBox& b = L.ba[n];
+            for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+                for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+                    for (int i = b.lo[0]; i <= b.hi[0]; ++i, ++off) {
+                        uint8_t t = 0;
+                        for (int c = 0; c < ntags; ++c) {
+                            const orc_tag& tg = tags[c];
+                            if (!(time >= tg.start_time && time <= tg.end_time) || lev >= tg.max_level) continue;
+                            if (tg.has_box) {
+                                const double x[3] = {L.plo[0] + (i + 0.5) * L.dx[0], L.plo[1] + (j + 0.5) * L.dx[1],
+                                                     L.plo[2] + (k + 0.5) * L.dx[2]};
+                                bool in = true;
+                                for (int d = 0; d < 3; ++d) in &= x[d] >= tg.box_lo[d] && x[d] <= tg.box_hi[d];
+                                if (!in) continue;
+                            }
+                            if (tg.kind == 0) { t = 1; continue; }
+                            const double v = tg.field == 19 ? (double)L.isf[n](i, j, k, 0) : L.md[n](i, j, k, tg.field);
+                            if ((tg.kind == 1 && v > tg.value) || (tg.kind == 2 && v < tg.value)) t = 1;
+                        }
+                        out[off] = t;
+                    }
+        }
+    }
+
+    // ---- regrid (LBM.cpp:1302-1364 RemakeLevel, 1088-1140 MakeNewLevelFromCoarse) --
+    // Levels first_lev.. get new box arrays (levels beyond the new ones are
+    // cleared).  A new level's valid cells take the old level's values where
+    // an old box held the cell, the coarse level's conservative-linear
+    // interpolation (interp_cell) elsewhere -- FillPatchTwoLevels over the new
+    // boxes -- then solid cells are zeroed (fill_f_inside_eb), ghosts refreshed
+    // and the macro data recomputed from the new state.
+    void regrid(int first_lev, const std::vector<std::vector<IBox>>& nb)
+    {
+        std::vector<Level> old(lv.begin() + first_lev, lv.end());
+        lv.resize(first_lev);
+        for (auto& pl : plans)
+            if ((int)pl.size() > first_lev) pl.resize(first_lev);
+        for (size_t m = 0; m < nb.size(); ++m) {
+            const int lev = first_lev + (int)m;
+            define_level(lev, nb[m]);
+            initialize_is_fluid(lev);
+            Level& L = lv[lev];
+            const Level& C = lv[lev - 1];
+            const Level* O = m < old.size() ? &old[m] : nullptr;
+            for (int lat = 0; lat < 2; ++lat) {
+                auto& mf = lat ? L.g : L.f;
+                const auto& cmf = lat ? C.g : C.f;
+                for (size_t n = 0; n < L.ba.size(); ++n) {
+                    auto& F = mf[n];
+                    const IBox b = L.ba[n];
+                    #pragma omp parallel for collapse(2) schedule(static)
+                    for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+                        for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+                            for (int i = b.lo[0]; i <= b.hi[0]; ++i) {
+                                int ob = -1;
+                                if (O)
+                                    for (size_t q = 0; q < O->ba.size() && ob < 0; ++q)
+                                        if (O->ba[q].contains(i, j, k)) ob = (int)q;
+                                if (ob >= 0) {
+                                    const auto& src = lat ? O->g[ob] : O->f[ob];
+                                    for (int q = 0; q < NQ; ++q) F(i, j, k, q) = src(i, j, k, q);
+                                } else {
+                                    double outv[NQ];
+                                    interp_cell(C, cmf, i, j, k, outv);
+                                    for (int q = 0; q < NQ; ++q) F(i, j, k, q) = outv[q];
+                                }
+                            }
+                }
+            }
+            for (size_t n = 0; n < L.ba.size(); ++n) {
+                const IBox b = L.ba[n];
+                for (int k = b.lo[2]; k <= b.hi[2]; ++k)
+                    for (int j = b.lo[1]; j <= b.hi[1]; ++j)
+                        for (int i = b.lo[0]; i <= b.hi[0]; ++i)
+                            if (L.isf[n](i, j, k, 0) == 0)
+                                for (int q = 0; q < NQ; ++q) { L.f[n](i, j, k, q) = 0.0; L.g[n](i, j, k, q) = 0.0; }
+            }
+            fill_boundary(L, L.f, NG);
+            fill_boundary(L, L.g, NG);
+            f_to_macrodata(lev);
+        }
+        compute_dt();
+    }
+
     // ---- driver (LBM.cpp:398-544) -----------------------------------------
     void init()
     {
@@ -1538,6 +1650,31 @@ int orc_collide_cell(void* h, const double* f, const double* g, const double* dq
                      double* go, double* qc)
 {
     static_cast<Sim*>(h)->collide_cell(f, g, dq, dt, fo, go, qc);
+    return 0;
+}
+
+// ErrorEst tags of level lev's valid cells ([box][k][j][i], 0/1)
+int orc_tag_cells(void* h, int lev, const orc_tag* tags, int ntags, double time, unsigned char* out)
+{
+    static_cast<Sim*>(h)->tag_level(lev, tags, ntags, time, out);
+    return 0;
+}
+
+// new box arrays for levels first_lev .. first_lev + nlev - 1 (nbox[m]
+// boxes each, lo/hi concatenated), the state remade as in RemakeLevel
+int orc_regrid(void* h, int first_lev, int nlev, const int* nbox, const int* lohi)
+{
+    auto* s = static_cast<Sim*>(h);
+    if (first_lev < 1 || first_lev > (int)s->lv.size()) return 1;
+    std::vector<std::vector<IBox>> nb(nlev);
+    size_t off = 0;
+    for (int m = 0; m < nlev; ++m)
+        for (int n = 0; n < nbox[m]; ++n, ++off) {
+            IBox b;
+            for (int d = 0; d < 3; ++d) { b.lo[d] = lohi[6 * off + d]; b.hi[d] = lohi[6 * off + 3 + d]; }
+            nb[m].push_back(b);
+        }
+    s->regrid(first_lev, nb);
     return 0;
 }
 

@@ -90,6 +90,8 @@ def lib():
         L.orc_stencil.argtypes = [ip, dp, ip, ip, ip, ip]
         L.orc_get_grown_flags.argtypes = [vp, C.c_int, C.POINTER(C.c_uint8)]
         L.orc_eb_forces.argtypes = [vp, dp]
+        L.orc_tag_cells.argtypes = [vp, C.c_int, C.POINTER(OrcTag), C.c_int, C.c_double, C.POINTER(C.c_uint8)]
+        L.orc_regrid.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.orc_equilibrium_cell.argtypes = [vp, C.c_double, dp, C.c_double, dp, dp]
         L.orc_collide_cell.argtypes = [vp, dp, dp, dp, C.c_double, dp, dp, dp]
         _lib = L
@@ -160,6 +162,25 @@ def chop_domain(n_cell, max_grid_size):
     return out.reshape(n, 6)
 
 
+class OrcTag(C.Structure):
+    """One refinement criterion (field: macro component 0..18 or 19 = is_fluid;
+    kind 0 box only, 1 value_greater, 2 value_less)."""
+    _fields_ = [("field", C.c_int), ("kind", C.c_int), ("value", C.c_double), ("has_box", C.c_int),
+                ("box_lo", C.c_double * 3), ("box_hi", C.c_double * 3), ("start_time", C.c_double),
+                ("end_time", C.c_double), ("max_level", C.c_int)]
+
+
+def make_tag(field=0, kind=1, value=0.0, box=None, start_time=-1.0e300, end_time=1.0e300, max_level=1000):
+    t = OrcTag()
+    t.field, t.kind, t.value = field, kind, value
+    t.has_box = 1 if box is not None else 0
+    if box is not None:
+        t.box_lo[:] = list(box[0])
+        t.box_hi[:] = list(box[1])
+    t.start_time, t.end_time, t.max_level = start_time, end_time, max_level
+    return t
+
+
 class Oracle:
     """One simulation: levels of boxes, FP64 f and g, the reference's step."""
 
@@ -227,6 +248,22 @@ class Oracle:
         out = np.zeros(3)
         self.L.orc_eb_forces(self.h, _dp(out))
         return out
+
+    def tag_cells(self, lev, tags, time):
+        """ErrorEst tags (0/1 per valid cell of level lev, [box][cell])."""
+        arr = (OrcTag * len(tags))(*tags)
+        out = np.zeros(self.ncells(lev), dtype=np.uint8)
+        self.L.orc_tag_cells(self.h, lev, arr, len(tags), time, out.ctypes.data_as(C.POINTER(C.c_uint8)))
+        return out
+
+    def regrid(self, first_lev, new_levels):
+        """Replace levels first_lev.. with the box arrays new_levels (RemakeLevel)."""
+        nbox = np.array([len(b) for b in new_levels] or [0], dtype=np.int32)
+        parts = [np.asarray(b, dtype=np.int32).reshape(-1) for b in new_levels]
+        lohi = np.ascontiguousarray(np.concatenate(parts) if parts else np.zeros(6, dtype=np.int32))
+        st = self.L.orc_regrid(self.h, first_lev, len(new_levels), _ip(nbox), _ip(lohi))
+        assert st == 0
+        self.levels = self.levels[:first_lev] + [np.ascontiguousarray(b, dtype=np.int32) for b in new_levels]
 
     def equilibrium_cell(self, rho, vel, temp):
         """f_eq, g_eq of one cell at (rho, vel, T) (the initializer's)."""
