@@ -55,6 +55,8 @@ struct Level {
     NbrSlot* d_slots = nullptr;
     Tile* d_fast_tiles = nullptr;
     int nfast = 0;
+    Tile* d_fasteb_tiles = nullptr;
+    int nfasteb = 0;
     Tile* d_gen_tiles = nullptr;
     int ngen = 0;
     GhostCell* d_ghost = nullptr;
@@ -324,6 +326,8 @@ static void refresh_plan(mbg_ctx* ctx, Level& L)
     L.plan.slots = L.d_slots;
     L.plan.fast_tiles = L.d_fast_tiles;
     L.plan.nfast = L.nfast;
+    L.plan.fasteb_tiles = L.d_fasteb_tiles;
+    L.plan.nfasteb = L.nfasteb;
     L.plan.gen_tiles = L.d_gen_tiles;
     L.plan.ngen = L.ngen;
     L.plan.ghost_list = L.d_ghost;
@@ -683,24 +687,30 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     MBG_CUDA(cudaMemcpyAsync(L.d_omap, L.omap.data(), L.omap.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     if ((st = dalloc(ctx, &L.d_flags, L.hflags.size())) != MBG_OK) return st;
     MBG_CUDA(cudaMemcpyAsync(L.d_flags, L.hflags.data(), L.hflags.size(), cudaMemcpyHostToDevice, ctx->s));
-    std::vector<Tile> tiles, fast_tiles, gen_tiles;
+    std::vector<Tile> tiles, fast_tiles, fasteb_tiles, gen_tiles;
     std::vector<NbrSlot> slots;
     build_slots(L, p.is_periodic, slots);
     for (int n = 0; n < nbox; ++n) {
-        bool simple = L.hbox[n].all_fluid != 0;
+        bool simple = true;
         for (int k = 0; k < 27 && simple; ++k) simple = slots[(size_t)n * 27 + k].ghost >= 0;
+        std::vector<Tile>& list = !simple ? gen_tiles : (L.hbox[n].all_fluid ? fast_tiles : fasteb_tiles);
         for (long long s = 0; s < L.boxes[n].vol(); s += TILE_CELLS) {
             tiles.push_back(Tile{n, (int)s});
-            (simple ? fast_tiles : gen_tiles).push_back(Tile{n, (int)s});
+            list.push_back(Tile{n, (int)s});
         }
     }
     L.ntiles = (int)tiles.size();
     L.nfast = (int)fast_tiles.size();
+    L.nfasteb = (int)fasteb_tiles.size();
     L.ngen = (int)gen_tiles.size();
     if ((st = dalloc(ctx, &L.d_tiles, tiles.size())) != MBG_OK) return st;
     MBG_CUDA(cudaMemcpyAsync(L.d_tiles, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, ctx->s));
     if ((st = dalloc(ctx, &L.d_fast_tiles, fast_tiles.size())) != MBG_OK) return st;
     if ((st = dalloc(ctx, &L.d_gen_tiles, gen_tiles.size())) != MBG_OK) return st;
+    if ((st = dalloc(ctx, &L.d_fasteb_tiles, fasteb_tiles.size())) != MBG_OK) return st;
+    if (!fasteb_tiles.empty())
+        MBG_CUDA(cudaMemcpyAsync(L.d_fasteb_tiles, fasteb_tiles.data(), fasteb_tiles.size() * sizeof(Tile),
+                                 cudaMemcpyHostToDevice, ctx->s));
     if ((st = dalloc(ctx, &L.d_slots, slots.size())) != MBG_OK) return st;
     if (!fast_tiles.empty())
         MBG_CUDA(cudaMemcpyAsync(L.d_fast_tiles, fast_tiles.data(), fast_tiles.size() * sizeof(Tile),

@@ -2,12 +2,14 @@
 // arithmetic).  Compiled with -fmad=false so that every multiply and add is
 // rounded separately, as in the reference's CPU build.
 //
-// A level advance is two passes over the valid cells, each launched over two
-// tile lists: boxes whose neighbourhood is plain (all fluid, no physical
+// A level advance is two passes over the valid cells, each launched over up
+// to three tile lists: boxes whose neighbourhood is plain (no physical
 // boundary within one cell, every neighbour region held by one box) pull by
 // a per-box table of 27 neighbour slots -- the same index arithmetic for
-// every cell, so warps do not diverge at box faces -- and the other boxes
-// through the general pull with its boundary cases:
+// every cell, so warps do not diverge at box faces -- without flag checks
+// when the box is all fluid and with them (bounce-back at solid sources)
+// when it holds solids; the other boxes use the general pull with its
+// boundary cases:
 //   k_moments : pull-stream f and g (Source/LBM.cpp:558-604) and compute the
 //               macro fields (f_to_macrodata, LBM.cpp:810-906) into a scratch
 //               array;
@@ -40,6 +42,19 @@ __device__ __forceinline__ double pull_slot(const NbrSlot* S, const DevBox& B, i
     return s.ghost ? vg[q * NG + i] : v[q * N + i];
 }
 
+// the same in a box holding solid cells: a solid source bounces back the
+// target's own opposite population (the half-way bounce-back of the push,
+// Source/LBM.cpp:574-598)
+template <int q>
+__device__ __forceinline__ double pull_slot_eb(const LV& L, const NbrSlot* S, const DevBox& B, int x, int y, int z,
+                                               const double* v, const double* vg)
+{
+    constexpr int oq = opp(q);
+    if (!(flag_at(L, B, x - ev_x(q), y - ev_y(q), z - ev_z(q)) & FL_FLUID))
+        return v[oq * L.N + B.voff + val_lin(B, x, y, z)];
+    return pull_slot<q>(S, B, x, y, z, v, vg, L.N, L.NG);
+}
+
 // Q_corr component d at box-local neighbour (x, y, z) through the slot map
 // (the macro scratch has the layout of the populations; the ghost fab's
 // Q_corr scratch that of the ghost fab)
@@ -54,16 +69,21 @@ __device__ __forceinline__ double qcorr_slot(const NbrSlot* S, const DevBox& B, 
     return s.ghost ? gqc[d * NG + i] : md[(MD_QCX + d) * N + i];
 }
 
-// gradient() of Source/Utilities.H:279-312 in an all-fluid box: one-sided
-// only at the domain box
+// gradient() of Source/Utilities.H:279-312 through the slot map: one-sided at
+// the domain box and, in boxes holding solids (EB), at solid neighbours
+template <bool EB>
 __device__ __forceinline__ double qgrad_slot(const LV& L, const NbrSlot* S, const DevBox& B, int x, int y, int z,
                                              int d, double idx, const double* md, const double* gqc)
 {
     int pp[3] = {x, y, z}, pm[3] = {x, y, z};
     pp[d] += 1;
     pm[d] -= 1;
-    const bool p_out = B.lo[d] + pp[d] > L.dhi[d];
-    const bool m_out = B.lo[d] + pm[d] < L.dlo[d];
+    bool p_out = B.lo[d] + pp[d] > L.dhi[d];
+    bool m_out = B.lo[d] + pm[d] < L.dlo[d];
+    if (EB) {
+        p_out = p_out || !(flag_at(L, B, pp[0], pp[1], pp[2]) & FL_FLUID);
+        m_out = m_out || !(flag_at(L, B, pm[0], pm[1], pm[2]) & FL_FLUID);
+    }
     double vp = 0.0, vc = 0.0, vm = 0.0;
     if (p_out && m_out) {
         vp = 0.0; vc = 0.0; vm = 0.0;
@@ -84,11 +104,11 @@ __device__ __forceinline__ double qgrad_slot(const LV& L, const NbrSlot* S, cons
 }
 
 // the CTA's tile: its box's slot map in shared memory, the thread's cell
-template <bool FAST>
+template <int MODE>
 __device__ __forceinline__ bool tile_setup(const LV& L, const LevelPlan& lp, const Tile* tiles, NbrSlot* sl, int& b,
                                            int& x, int& y, int& z, long long& c)
 {
-    if (FAST) {
+    if (MODE > 0) {
         const int box = tiles[blockIdx.x].box;
         if (threadIdx.x < 27) sl[threadIdx.x] = lp.slots[(long long)box * 27 + threadIdx.x];
         __syncthreads();
@@ -97,7 +117,9 @@ __device__ __forceinline__ bool tile_setup(const LV& L, const LevelPlan& lp, con
 }
 
 // ---- pass 1: stream + macro fields ----------------------------------------
-template <bool FAST>
+// MODE 0: general pull; 1: neighbour slots, all-fluid box; 2: neighbour
+// slots, box holding solid cells
+template <int MODE>
 __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, LevelPlan lp, BCParams P, Phys64 ph, const Tile* tiles,
                                                         const double* fA, const double* gA, const double* fAg,
                                                         const double* gAg, const double* fB, const double* gB,
@@ -106,7 +128,7 @@ __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, LevelPlan lp, BCPa
     __shared__ NbrSlot sl[27];
     int b, x, y, z;
     long long c;
-    if (!tile_setup<FAST>(L, lp, tiles, sl, b, x, y, z, c)) return;
+    if (!tile_setup<MODE>(L, lp, tiles, sl, b, x, y, z, c)) return;
     const DevBox& B = L.box[b];
     const uint8_t tf = flag_at(L, B, x, y, z);
     if (!(tf & FL_FLUID)) return;
@@ -114,10 +136,12 @@ __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, LevelPlan lp, BCPa
     const bool interior = !ovr && is_interior(B, x, y, z);
     const long long cell = B.voff + c;
     MomentAcc<double> acc;
-#define MBG_PULLF(q) (FAST ? pull_slot<q>(sl, B, x, y, z, fA, fAg, L.N, L.NG) \
-                           : pull<q>(L, P, B, x, y, z, tf, interior, fA, fAg, false, ph.lat))
-#define MBG_PULLG(q) (FAST ? pull_slot<q>(sl, B, x, y, z, gA, gAg, L.N, L.NG) \
-                           : pull<q>(L, P, B, x, y, z, tf, interior, gA, gAg, true, ph.lat))
+#define MBG_PULLF(q) (MODE == 1 ? pull_slot<q>(sl, B, x, y, z, fA, fAg, L.N, L.NG)                  \
+                     : MODE == 2 ? pull_slot_eb<q>(L, sl, B, x, y, z, fA, fAg)                       \
+                                 : pull<q>(L, P, B, x, y, z, tf, interior, fA, fAg, false, ph.lat))
+#define MBG_PULLG(q) (MODE == 1 ? pull_slot<q>(sl, B, x, y, z, gA, gAg, L.N, L.NG)                  \
+                     : MODE == 2 ? pull_slot_eb<q>(L, sl, B, x, y, z, gA, gAg)                       \
+                                 : pull<q>(L, P, B, x, y, z, tf, interior, gA, gAg, true, ph.lat))
 #define MBG_M64(q)                                                             \
     {                                                                          \
         double fq = ovr ? fB[q * L.N + cell] : 0.0;                            \
@@ -151,7 +175,7 @@ __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, LevelPlan lp, BCPa
 }
 
 // ---- pass 2: q-correction, equilibria, relaxation --------------------------
-template <bool FAST>
+template <int MODE>
 __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, LevelPlan lp, BCParams P, Phys64 ph, const Tile* tiles,
                                                         const double* fA, const double* gA, const double* fAg,
                                                         const double* gAg, double* fB, double* gB,
@@ -160,7 +184,7 @@ __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, LevelPlan lp, BCPa
     __shared__ NbrSlot sl[27];
     int b, x, y, z;
     long long c;
-    if (!tile_setup<FAST>(L, lp, tiles, sl, b, x, y, z, c)) return;
+    if (!tile_setup<MODE>(L, lp, tiles, sl, b, x, y, z, c)) return;
     const DevBox& B = L.box[b];
     const uint8_t tf = flag_at(L, B, x, y, z);
     const long long N = L.N;
@@ -193,10 +217,10 @@ __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, LevelPlan lp, BCPa
     m.qz = md[MD_QZ * N + cell];
     m.temp = md[MD_T * N + cell];
     double dqx, dqy, dqz;
-    if (FAST) {
-        dqx = qgrad_slot(L, sl, B, x, y, z, 0, ph.idx[0], md, gqc);
-        dqy = qgrad_slot(L, sl, B, x, y, z, 1, ph.idx[1], md, gqc);
-        dqz = qgrad_slot(L, sl, B, x, y, z, 2, ph.idx[2], md, gqc);
+    if (MODE > 0) {
+        dqx = qgrad_slot<MODE == 2>(L, sl, B, x, y, z, 0, ph.idx[0], md, gqc);
+        dqy = qgrad_slot<MODE == 2>(L, sl, B, x, y, z, 1, ph.idx[1], md, gqc);
+        dqz = qgrad_slot<MODE == 2>(L, sl, B, x, y, z, 2, ph.idx[2], md, gqc);
     } else {
         dqx = qgrad(L, B, x, y, z, 0, ph.idx[0], md, gqc);
         dqy = qgrad(L, B, x, y, z, 1, ph.idx[1], md, gqc);
@@ -234,11 +258,14 @@ void launch_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, co
                     cudaStream_t s)
 {
     if (lp.nfast > 0)
-        k_moments<true><<<lp.nfast, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB,
-                                                       gB, md);
+        k_moments<1><<<lp.nfast, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB, gB,
+                                                    md);
+    if (lp.nfasteb > 0)
+        k_moments<2><<<lp.nfasteb, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fasteb_tiles, fA, gA, fAg, gAg, fB,
+                                                      gB, md);
     if (lp.ngen > 0)
-        k_moments<false><<<lp.ngen, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB,
-                                                        gB, md);
+        k_moments<0><<<lp.ngen, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB, gB,
+                                                   md);
 }
 
 void launch_collide(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
@@ -246,13 +273,16 @@ void launch_collide(const LevelPlan& lp, const BCParams& P, const Phys64& ph, co
                     const double* gqc, cudaStream_t s)
 {
     if (lp.nfast > 0)
-        k_collide<true><<<lp.nfast, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB,
-                                                       gB, md, gqc);
+        k_collide<1><<<lp.nfast, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB, gB,
+                                                    md, gqc);
+    if (lp.nfasteb > 0)
+        k_collide<2><<<lp.nfasteb, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fasteb_tiles, fA, gA, fAg, gAg, fB,
+                                                      gB, md, gqc);
     if (lp.ngen > 0)
-        k_collide<false><<<lp.ngen, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB,
-                                                        gB, md, gqc);
+        k_collide<0><<<lp.ngen, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB, gB,
+                                                   md, gqc);
 }
 
-int fp64_step_launches(const LevelPlan& lp) { return (lp.nfast > 0) + (lp.ngen > 0); }
+int fp64_step_launches(const LevelPlan& lp) { return (lp.nfast > 0) + (lp.nfasteb > 0) + (lp.ngen > 0); }
 
 }  // namespace mbg

@@ -83,6 +83,8 @@ struct LevelPlan {
     const NbrSlot* slots = nullptr;   // [box][27]
     const Tile* fast_tiles = nullptr;
     int nfast = 0;
+    const Tile* fasteb_tiles = nullptr;   // the same for boxes holding solid cells
+    int nfasteb = 0;
     const Tile* gen_tiles = nullptr;
     int ngen = 0;
     const GhostCell* ghost_list = nullptr;   // all uncovered ghost cells

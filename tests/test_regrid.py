@@ -131,17 +131,29 @@ def test_regrid_16bit_forms(prec):
             off += 19 * vol
 
 
-def test_driver_regrid_continues_like_the_oracle():
-    """Field tagging (rho value_greater) picks the fine level from the
-    initial state; after 3 steps an explicit regrid moves it; the oracle,
-    given the driver's grids at the same points, ends in the same state."""
+def _moving_inputs():
+    """The 32^3 pulse with tagging on state fields and time windows: rho >
+    1.0015 until t = 2 (the fine level around the pulse, tagged on the initial
+    state), then rho > 1.0005 and a box towards the low corner from t = 3:
+    the fine level must move and grow at a regrid after step 3."""
     import inputs
-    import marbles_gb300 as M
     text = inputs.pulse(nc=32, lo=8, hi=24, mgs=16, width=3.0, t0=0.1)
-    text = text.replace("tagging.refinement_indicators = centre",
-                        "tagging.refinement_indicators = hi\ntagging.hi.field_name = rho\n"
-                        "tagging.hi.value_greater = 1.0015")
-    d = M.LBM(text)
+    return text.replace("tagging.refinement_indicators = centre",
+                        "tagging.refinement_indicators = early late corner\n"
+                        "tagging.early.field_name = rho\ntagging.early.value_greater = 1.0015\n"
+                        "tagging.early.end_time = 2.0\n"
+                        "tagging.late.field_name = rho\ntagging.late.value_greater = 1.0005\n"
+                        "tagging.late.start_time = 3.0\n"
+                        "tagging.corner.in_box_lo = 6.0 6.0 8.0\ntagging.corner.in_box_hi = 10.0 9.0 12.0\n"
+                        "tagging.corner.start_time = 3.0")
+
+
+def test_driver_regrid_continues_like_the_oracle():
+    """Field tagging picks the fine level from the initial state; after 3
+    steps an explicit regrid moves it; the oracle, given the driver's grids at
+    the same points, ends in the same state."""
+    import marbles_gb300 as M
+    d = M.LBM(_moving_inputs())
     ctx = d.init()
     g0 = [d.boxes(l) for l in range(d.num_levels())]
     assert len(g0) == 2
@@ -161,13 +173,8 @@ def test_driver_regrid_continues_like_the_oracle():
 
 
 def test_driver_regrid_interval():
-    import inputs
     import marbles_gb300 as M
-    text = inputs.pulse(nc=32, lo=8, hi=24, mgs=16, width=3.0, t0=0.1)
-    text = text.replace("tagging.refinement_indicators = centre",
-                        "tagging.refinement_indicators = hi\ntagging.hi.field_name = rho\n"
-                        "tagging.hi.value_greater = 1.0015")
-    text = text.replace("amr.regrid_int = 1000000", "amr.regrid_int = 2")
+    text = _moving_inputs().replace("amr.regrid_int = 1000000", "amr.regrid_int = 2")
     d = M.LBM(text)
     ctx = d.init()
     n0 = sum(int(np.prod(b[3:] - b[:3] + 1)) for b in d.boxes(1))
