@@ -1,7 +1,9 @@
 // mbg_fp64_amr.cu -- FP64 level-to-level transfers: explosion of the coarse
 // level into a fine level's ghost shell and coalescence of the fine level onto
 // the coarse level.
+#include <cmath>
 #include <cstdio>
+#include <cstring>
 
 #include "mbg_fp64.cuh"
 
@@ -118,7 +120,24 @@ __global__ void k_xfill(LV F, const GhostCell* __restrict__ gl, const int* __res
 // child is masked (the step then pulls the coarse cell's own streamed value).  One thread per (coarse cell, direction):
 // blockIdx.y is the direction, so a warp reads one component of 32
 // consecutive coarse cells' children.
-__global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, const CoalesceCell* cl, long long n,
+// The mask test |v - (-1)| > SMALL_NUM of masked_avgdown without FP64
+// arithmetic: v - (-1) is exact for v in [-2, -0.5] (Sterbenz) and at least
+// 0.5 in magnitude elsewhere, so a child is masked exactly when v is NaN or
+// lies in [lo, hi], lo the smallest double >= -1 - SMALL_NUM and hi the
+// largest <= SMALL_NUM - 1 (both negative, found exactly on the host).  For
+// negative doubles the unsigned bit pattern grows with the magnitude.
+struct MaskBits {
+    unsigned long long lo, hi;   // bit patterns of lo (the larger) and hi
+};
+
+__device__ __forceinline__ bool child_masked(double v, const MaskBits& mb)
+{
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const bool nan = (u & 0x7FFFFFFFFFFFFFFFULL) > 0x7FF0000000000000ULL;
+    return nan || (u >= mb.hi && u <= mb.lo);
+}
+
+__global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, MaskBits mb, const CoalesceCell* cl, long long n,
                            const double* ff, const double* gf, const double* ffg, const double* gfg,
                            const double* fcA, const double* gcA, const double* fcAg, const double* gcAg,
                            double* fcB, double* gcB, int into_state)
@@ -130,14 +149,14 @@ __global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, const CoalesceCell
     const DevBox& O = C.box[cc.cbox];
     const DevBox& A = F.box[cc.fbox];
     const long long cell = O.voff + val_lin(O, cc.cx, cc.cy, cc.cz);
-    const double masked = -1.0;
     const bool inA = cc.fx >= 0 && cc.fy >= 0 && cc.fz >= 0 && cc.fx + 1 < A.n[0] && cc.fy + 1 < A.n[1] &&
                      cc.fz + 1 < A.n[2];
     for (int lat = 0; lat < 2; ++lat) {
         const double* v = lat ? gf : ff;
         const double* vg = lat ? gfg : ffg;
         const double* cA = lat ? gcA : fcA;
-        double s = 0.0, vol = 0.0;
+        double s = 0.0;
+        int cnt = 0;   // children kept; the reference's FP64 count 1.0, 2.0, ... exactly
         if (inA) {
             // the eight children are valid cells of box A: fixed offsets
             const double* c0 = v + (long long)q * F.N + A.voff + val_lin(A, cc.fx, cc.fy, cc.fz);
@@ -145,18 +164,18 @@ __global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, const CoalesceCell
                 for (int jr = 0; jr < 2; ++jr)
                     for (int ir = 0; ir < 2; ++ir) {
                         const double fv = c0[kr * A.sz + jr * A.sy + ir];
-                        if (fabs(fv - masked) > ph.small_num) { s += fv; vol += 1.0; }
+                        if (!child_masked(fv, mb)) { s += fv; ++cnt; }
                     }
         } else {
             for (int kr = 0; kr < 2; ++kr)
                 for (int jr = 0; jr < 2; ++jr)
                     for (int ir = 0; ir < 2; ++ir) {
                         const double fv = fab_value(F, A, cc.fx + ir, cc.fy + jr, cc.fz + kr, q, v, vg);
-                        if (fabs(fv - masked) > ph.small_num) { s += fv; vol += 1.0; }
+                        if (!child_masked(fv, mb)) { s += fv; ++cnt; }
                     }
         }
         double r;
-        if (vol > 0.0) r = s / vol;
+        if (cnt > 0) r = s / (double)cnt;
         else if (into_state) r = cA[q * C.N + cell];
         else r = __longlong_as_double(NOOVR64);   // the step pulls the cell's own streamed value
         (lat ? gcB : fcB)[q * C.N + cell] = r;
@@ -174,6 +193,27 @@ void launch_explode(const LevelPlan& fine, const LevelPlan& crse, const double* 
         fine.view64, fine.ghost_list, fine.xslot, fine.nghost_cells, fine.xs, fine.xal, fine.nx, fg, gg);
 }
 
+// lo = the smallest double >= -1 - t and hi = the largest double <= t - 1
+// (t = SMALL_NUM > 0, tiny), from an exact TwoSum of each rounded sum
+static MaskBits mask_bits(double t)
+{
+    auto two_sum = [](double a, double b, double& err) {
+        const double s = a + b;
+        const double bb = s - a;
+        err = (a - (s - bb)) + (b - bb);
+        return s;
+    };
+    double e;
+    double lo = two_sum(-1.0, -t, e);
+    if (e > 0.0) lo = std::nextafter(lo, 0.0);             // the real sum lies above the rounded one
+    double hi = two_sum(t, -1.0, e);
+    if (e < 0.0) hi = std::nextafter(hi, -2.0);            // the real sum lies below the rounded one
+    MaskBits mb;
+    std::memcpy(&mb.lo, &lo, sizeof lo);
+    std::memcpy(&mb.hi, &hi, sizeof hi);
+    return mb;
+}
+
 void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParams& P, const Phys64& ph,
                      const CoalesceCell* list, long long n, const double* ff, const double* gf, const double* ffg,
                      const double* gfg, const double* fcA, const double* gcA, const double* fcAg,
@@ -182,8 +222,8 @@ void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParam
     if (n == 0) return;
     const int th = 128;
     const dim3 grid((unsigned)((n + th - 1) / th), NQ);
-    k_coalesce<<<grid, th, 0, s>>>(crse.view64, fine.view64, P, ph, list, n, ff, gf, ffg, gfg, fcA, gcA,
-                                           fcAg, gcAg, fcB, gcB, into_state);
+    k_coalesce<<<grid, th, 0, s>>>(crse.view64, fine.view64, P, ph, mask_bits(ph.small_num), list, n, ff, gf, ffg,
+                                   gfg, fcA, gcA, fcAg, gcAg, fcB, gcB, into_state);
 }
 
 // ---- regrid: every cell of a new fine level from the coarse level ----------
