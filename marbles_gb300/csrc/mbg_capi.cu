@@ -921,7 +921,7 @@ static mbg_status advance(mbg_ctx* ctx, int lev)
             launch_ghost_stream(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.fg[Bf], L.gg[Bf], ctx->s);
         });
         timed(ctx, TK_GHOST_MOMENTS, [&] {
-            launch_ghost_moments(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.gqc, ctx->s);
+            launch_ghost_moments(L.plan, ph, L.fg[Bf], L.gg[Bf], L.gqc, ctx->s);
         });
         ctx->launches += 2;
     }

@@ -130,8 +130,10 @@ int fp64_step_launches(const LevelPlan& lp);
 void launch_ghost_stream(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA,
                          const double* gA, const double* fAg, const double* gAg, double* fBg, double* gBg,
                          cudaStream_t s);
-void launch_ghost_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA,
-                          const double* gA, const double* fAg, const double* gAg, double* gqc, cudaStream_t s);
+// Q_corr of the first-layer ghost cells from the ghost fab that
+// launch_ghost_stream has just written (fBg, gBg)
+void launch_ghost_moments(const LevelPlan& lp, const Phys64& ph, const double* fBg, const double* gBg, double* gqc,
+                          cudaStream_t s);
 void launch_explode(const LevelPlan& fine, const LevelPlan& crse, const double* fc, const double* gc, double* fg,
                     double* gg, cudaStream_t s);
 void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParams& P, const Phys64& ph,
