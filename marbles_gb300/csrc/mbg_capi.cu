@@ -53,6 +53,9 @@ struct Level {
     Tile* d_tiles = nullptr;
     int ntiles = 0;
     NbrSlot* d_slots = nullptr;
+    int* d_slot_off = nullptr;
+    int slot_lg[3] = {0, 0, 0};
+    int slot_max = 0;
     Tile* d_fast_tiles = nullptr;
     int nfast = 0;
     Tile* d_fasteb_tiles = nullptr;
@@ -242,35 +245,63 @@ static int owner_host(const Level& L, const int p[3])
     return L.omap[((size_t)bk * L.nb[1] + bj) * L.nb[0] + bi];
 }
 
-// The 27 neighbour regions of every box (NbrSlot): a region maps to one box
-// when all its cells (after the periodic wrap) lie in that box's valid
-// cells at one fixed offset, or to the box's ghost fab when none lies in a
-// box and the box has one; ghost = -1 marks a region that maps to neither
-// (a non-periodic domain side, several boxes, covered and uncovered cells).
-static void build_slots(const Level& L, const int* is_periodic, std::vector<NbrSlot>& out)
+// Neighbour-slot tables of every box (NbrSlot): a chunk maps to one box when
+// all its cells (after the periodic wrap) lie in that box's valid cells at
+// one fixed offset, or to the box's ghost fab when none lies in a box and the
+// box has one.  ok[n] is set when every chunk of box n maps (no non-periodic
+// domain side within one cell, no chunk across a box edge) and its table
+// fits; off[n] is the table's first slot, -1 for a box without one.
+static void build_slots(const Level& L, const int* is_periodic, const int lg[3], std::vector<NbrSlot>& out,
+                        std::vector<int>& off, std::vector<char>& ok)
 {
     const int nbox = (int)L.boxes.size();
-    out.assign((size_t)nbox * 27, NbrSlot{0, 0, 0, -1, 0});
+    out.clear();
+    off.assign(nbox, -1);
+    ok.assign(nbox, 0);
     for (int n = 0; n < nbox; ++n) {
         const HBox& b = L.boxes[n];
         const DevBox& B = L.hbox[n];
-        for (int oz = 0; oz < 3; ++oz)
-            for (int oy = 0; oy < 3; ++oy)
-                for (int ox = 0; ox < 3; ++ox) {
-                    const int o3[3] = {ox, oy, oz};
+        int nch[3], tc[3];
+        for (int d = 0; d < 3; ++d) {
+            nch[d] = (b.n(d) + (1 << lg[d]) - 1) >> lg[d];
+            tc[d] = nch[d] + 2;
+        }
+        const long long T = (long long)tc[0] * tc[1] * tc[2];
+        if (T > SLOT_TABLE_MAX) continue;
+        const size_t t0 = out.size();
+        out.resize(t0 + (size_t)T, NbrSlot{0, 0, 0, -1, 0});
+        bool all = true;
+        for (int cz = 0; cz < tc[2]; ++cz)
+            for (int cy = 0; cy < tc[1]; ++cy)
+                for (int cx = 0; cx < tc[0]; ++cx) {
+                    const int c3[3] = {cx, cy, cz};
+                    NbrSlot& S = out[t0 + cx + (size_t)tc[0] * (cy + (size_t)tc[1] * cz)];
                     int rlo[3], rhi[3];
+                    bool inside = true;
                     for (int d = 0; d < 3; ++d) {
-                        rlo[d] = o3[d] == 0 ? -1 : (o3[d] == 1 ? 0 : b.n(d));
-                        rhi[d] = o3[d] == 0 ? -1 : (o3[d] == 1 ? b.n(d) - 1 : b.n(d));
+                        if (c3[d] == 0) rlo[d] = rhi[d] = -1;
+                        else if (c3[d] == tc[d] - 1) rlo[d] = rhi[d] = b.n(d);
+                        else {
+                            rlo[d] = (c3[d] - 1) << lg[d];
+                            rhi[d] = std::min(c3[d] << lg[d], b.n(d)) - 1;
+                        }
+                        inside = inside && c3[d] > 0 && c3[d] < tc[d] - 1;
+                    }
+                    if (inside) {   // the box itself
+                        S.base = B.voff;
+                        S.sy = B.sy;
+                        S.sz = B.sz;
+                        S.ghost = 0;
+                        continue;
                     }
                     int owner = -2;         // -2: unset, -1: uncovered
                     int delta[3] = {0, 0, 0};
-                    bool ok = true;
-                    for (int z = rlo[2]; z <= rhi[2] && ok; ++z)
-                        for (int y = rlo[1]; y <= rhi[1] && ok; ++y)
-                            for (int x = rlo[0]; x <= rhi[0] && ok; ++x) {
+                    bool good = true;
+                    for (int z = rlo[2]; z <= rhi[2] && good; ++z)
+                        for (int y = rlo[1]; y <= rhi[1] && good; ++y)
+                            for (int x = rlo[0]; x <= rhi[0] && good; ++x) {
                                 int gp[3] = {b.lo[0] + x, b.lo[1] + y, b.lo[2] + z};
-                                if (!wrap_host(L, is_periodic, gp)) { ok = false; break; }
+                                if (!wrap_host(L, is_periodic, gp)) { good = false; break; }
                                 const int o = owner_host(L, gp);
                                 int dl[3] = {0, 0, 0};
                                 if (o >= 0) {
@@ -282,26 +313,41 @@ static void build_slots(const Level& L, const int* is_periodic, std::vector<NbrS
                                     owner = o;
                                     for (int d = 0; d < 3; ++d) delta[d] = dl[d];
                                 } else if (o != owner || dl[0] != delta[0] || dl[1] != delta[1] || dl[2] != delta[2]) {
-                                    ok = false;
+                                    good = false;
                                 }
                             }
-                    NbrSlot& S = out[(size_t)n * 27 + ox + 3 * oy + 9 * oz];
-                    if (!ok) continue;
-                    if (owner >= 0) {
+                    if (good && owner >= 0) {
                         const DevBox& O = L.hbox[owner];
                         S.base = O.voff + (long long)delta[2] * O.sz + (long long)delta[1] * O.sy + delta[0];
                         S.sy = O.sy;
                         S.sz = O.sz;
                         S.ghost = 0;
-                    } else if (B.goff >= 0) {
+                    } else if (good && B.goff >= 0) {
                         const int gx = B.n[0] + 6, gy = B.n[1] + 6;
                         S.base = B.goff + 3LL * gy * gx + 3LL * gx + 3;
                         S.sy = gx;
                         S.sz = gx * gy;
                         S.ghost = 1;
+                    } else {
+                        all = false;
                     }
                 }
+        if (!all) {
+            out.resize(t0);
+            continue;
+        }
+        off[n] = (int)t0;
+        ok[n] = 1;
     }
+}
+
+// chunk length of the slot tables along d: the largest power of two, at most
+// 32, dividing the level's owner-map grain (every box corner and length)
+static int slot_lg(const Level& L, int d)
+{
+    int lg = 0;
+    while (lg < 5 && L.G[d] % (2 << lg) == 0) ++lg;
+    return lg;
 }
 
 static void refresh_plan(mbg_ctx* ctx, Level& L)
@@ -324,6 +370,9 @@ static void refresh_plan(mbg_ctx* ctx, Level& L)
     L.plan.tiles = L.d_tiles;
     L.plan.ntiles = L.ntiles;
     L.plan.slots = L.d_slots;
+    L.plan.slot_off = L.d_slot_off;
+    for (int d = 0; d < 3; ++d) L.plan.slot_lg[d] = L.slot_lg[d];
+    L.plan.slot_max = L.slot_max;
     L.plan.fast_tiles = L.d_fast_tiles;
     L.plan.nfast = L.nfast;
     L.plan.fasteb_tiles = L.d_fasteb_tiles;
@@ -689,10 +738,18 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     MBG_CUDA(cudaMemcpyAsync(L.d_flags, L.hflags.data(), L.hflags.size(), cudaMemcpyHostToDevice, ctx->s));
     std::vector<Tile> tiles, fast_tiles, fasteb_tiles, gen_tiles;
     std::vector<NbrSlot> slots;
-    build_slots(L, p.is_periodic, slots);
+    std::vector<int> slot_off;
+    std::vector<char> slot_ok;
+    for (int d = 0; d < 3; ++d) L.slot_lg[d] = slot_lg(L, d);
+    build_slots(L, p.is_periodic, L.slot_lg, slots, slot_off, slot_ok);
+    L.slot_max = 0;
     for (int n = 0; n < nbox; ++n) {
-        bool simple = true;
-        for (int k = 0; k < 27 && simple; ++k) simple = slots[(size_t)n * 27 + k].ghost >= 0;
+        const bool simple = slot_ok[n];
+        if (simple) {
+            int t = 1;
+            for (int d = 0; d < 3; ++d) t *= ((L.boxes[n].n(d) + (1 << L.slot_lg[d]) - 1) >> L.slot_lg[d]) + 2;
+            L.slot_max = std::max(L.slot_max, t);
+        }
         std::vector<Tile>& list = !simple ? gen_tiles : (L.hbox[n].all_fluid ? fast_tiles : fasteb_tiles);
         for (long long s = 0; s < L.boxes[n].vol(); s += TILE_CELLS) {
             tiles.push_back(Tile{n, (int)s});
@@ -718,7 +775,12 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     if (!gen_tiles.empty())
         MBG_CUDA(cudaMemcpyAsync(L.d_gen_tiles, gen_tiles.data(), gen_tiles.size() * sizeof(Tile),
                                  cudaMemcpyHostToDevice, ctx->s));
-    MBG_CUDA(cudaMemcpyAsync(L.d_slots, slots.data(), slots.size() * sizeof(NbrSlot), cudaMemcpyHostToDevice, ctx->s));
+    if (!slots.empty())
+        MBG_CUDA(cudaMemcpyAsync(L.d_slots, slots.data(), slots.size() * sizeof(NbrSlot), cudaMemcpyHostToDevice,
+                                 ctx->s));
+    if ((st = dalloc(ctx, &L.d_slot_off, slot_off.size())) != MBG_OK) return st;
+    MBG_CUDA(cudaMemcpyAsync(L.d_slot_off, slot_off.data(), slot_off.size() * sizeof(int), cudaMemcpyHostToDevice,
+                             ctx->s));
     L.nghost = (long long)ghosts.size();
     L.nghost1 = (long long)ghosts1.size();
     if ((st = dalloc(ctx, &L.d_ghost, ghosts.size())) != MBG_OK) return st;

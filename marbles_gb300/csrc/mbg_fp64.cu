@@ -4,9 +4,10 @@
 //
 // A level advance is two passes over the valid cells, each launched over up
 // to three tile lists: boxes whose neighbourhood is plain (no physical
-// boundary within one cell, every neighbour region held by one box) pull by
-// a per-box table of 27 neighbour slots -- the same index arithmetic for
-// every cell, so warps do not diverge at box faces -- without flag checks
+// boundary within one cell, every neighbour chunk held by one box or by the
+// box's ghost fab) pull by a per-box table of neighbour slots -- the same
+// index arithmetic for every cell, so warps do not diverge at box faces,
+// also on the uneven boxes of refined levels -- without flag checks
 // when the box is all fluid and with them (bounce-back at solid sources)
 // when it holds solids; the other boxes use the general pull with its
 // boundary cases:
@@ -25,19 +26,33 @@
 
 namespace mbg {
 
-// ---- pulls through the neighbour-slot map of the CTA's box -----------------
-// (boxes of the fast tile list: all fluid, no physical boundary within one
-// cell, every neighbour region in one box or in the box's ghost fab)
+// ---- pulls through the neighbour-slot table of the CTA's box ---------------
+// the table in shared memory and the chunking of the box
+struct SlotTab {
+    const NbrSlot* s;
+    int lg[3];
+    int tx, ty;      // table extent along x and y
+    int top[3];      // chunk index of the layer above the box
+};
+
+// chunk index along one axis of box-local coordinate v (-1 .. n)
+__device__ __forceinline__ int chunk_of(int v, int n, int lg, int top)
+{
+    return v < 0 ? 0 : (v < n ? (v >> lg) + 1 : top);
+}
+
+// (boxes of the slot tile lists: no physical boundary within one cell, every
+// neighbour chunk in one box or in the box's ghost fab)
 template <int q>
-__device__ __forceinline__ double pull_slot(const NbrSlot* S, const DevBox& B, int x, int y, int z,
+__device__ __forceinline__ double pull_slot(const SlotTab& T, const DevBox& B, int x, int y, int z,
                                             const double* v, const double* vg, long long N, long long NG)
 {
     constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
     const int sx = x - ex, sy = y - ey, sz = z - ez;
-    const int ox = ex == 0 ? 1 : (sx < 0 ? 0 : (sx < B.n[0] ? 1 : 2));
-    const int oy = ey == 0 ? 1 : (sy < 0 ? 0 : (sy < B.n[1] ? 1 : 2));
-    const int oz = ez == 0 ? 1 : (sz < 0 ? 0 : (sz < B.n[2] ? 1 : 2));
-    const NbrSlot& s = S[ox + 3 * oy + 9 * oz];
+    const int ox = ex == 0 ? (x >> T.lg[0]) + 1 : chunk_of(sx, B.n[0], T.lg[0], T.top[0]);
+    const int oy = ey == 0 ? (y >> T.lg[1]) + 1 : chunk_of(sy, B.n[1], T.lg[1], T.top[1]);
+    const int oz = ez == 0 ? (z >> T.lg[2]) + 1 : chunk_of(sz, B.n[2], T.lg[2], T.top[2]);
+    const NbrSlot& s = T.s[ox + T.tx * (oy + T.ty * oz)];
     const long long i = s.base + (long long)sz * s.sz + (long long)sy * s.sy + sx;
     return s.ghost ? vg[q * NG + i] : v[q * N + i];
 }
@@ -46,33 +61,33 @@ __device__ __forceinline__ double pull_slot(const NbrSlot* S, const DevBox& B, i
 // target's own opposite population (the half-way bounce-back of the push,
 // Source/LBM.cpp:574-598)
 template <int q>
-__device__ __forceinline__ double pull_slot_eb(const LV& L, const NbrSlot* S, const DevBox& B, int x, int y, int z,
+__device__ __forceinline__ double pull_slot_eb(const LV& L, const SlotTab& T, const DevBox& B, int x, int y, int z,
                                                const double* v, const double* vg)
 {
     constexpr int oq = opp(q);
     if (!(flag_at(L, B, x - ev_x(q), y - ev_y(q), z - ev_z(q)) & FL_FLUID))
         return v[oq * L.N + B.voff + val_lin(B, x, y, z)];
-    return pull_slot<q>(S, B, x, y, z, v, vg, L.N, L.NG);
+    return pull_slot<q>(T, B, x, y, z, v, vg, L.N, L.NG);
 }
 
-// Q_corr component d at box-local neighbour (x, y, z) through the slot map
+// Q_corr component d at box-local neighbour (x, y, z) through the slot table
 // (the macro scratch has the layout of the populations; the ghost fab's
 // Q_corr scratch that of the ghost fab)
-__device__ __forceinline__ double qcorr_slot(const NbrSlot* S, const DevBox& B, int x, int y, int z, int d,
+__device__ __forceinline__ double qcorr_slot(const SlotTab& T, const DevBox& B, int x, int y, int z, int d,
                                              const double* md, const double* gqc, long long N, long long NG)
 {
-    const int ox = x < 0 ? 0 : (x < B.n[0] ? 1 : 2);
-    const int oy = y < 0 ? 0 : (y < B.n[1] ? 1 : 2);
-    const int oz = z < 0 ? 0 : (z < B.n[2] ? 1 : 2);
-    const NbrSlot& s = S[ox + 3 * oy + 9 * oz];
+    const int ox = chunk_of(x, B.n[0], T.lg[0], T.top[0]);
+    const int oy = chunk_of(y, B.n[1], T.lg[1], T.top[1]);
+    const int oz = chunk_of(z, B.n[2], T.lg[2], T.top[2]);
+    const NbrSlot& s = T.s[ox + T.tx * (oy + T.ty * oz)];
     const long long i = s.base + (long long)z * s.sz + (long long)y * s.sy + x;
     return s.ghost ? gqc[d * NG + i] : md[(MD_QCX + d) * N + i];
 }
 
-// gradient() of Source/Utilities.H:279-312 through the slot map: one-sided at
-// the domain box and, in boxes holding solids (EB), at solid neighbours
+// gradient() of Source/Utilities.H:279-312 through the slot table: one-sided
+// at the domain box and, in boxes holding solids (EB), at solid neighbours
 template <bool EB>
-__device__ __forceinline__ double qgrad_slot(const LV& L, const NbrSlot* S, const DevBox& B, int x, int y, int z,
+__device__ __forceinline__ double qgrad_slot(const LV& L, const SlotTab& T, const DevBox& B, int x, int y, int z,
                                              int d, double idx, const double* md, const double* gqc)
 {
     int pp[3] = {x, y, z}, pm[3] = {x, y, z};
@@ -89,28 +104,41 @@ __device__ __forceinline__ double qgrad_slot(const LV& L, const NbrSlot* S, cons
         vp = 0.0; vc = 0.0; vm = 0.0;
     } else if (p_out) {
         vp = 0.0;
-        vc = qcorr_slot(S, B, x, y, z, d, md, gqc, L.N, L.NG);
-        vm = -qcorr_slot(S, B, pm[0], pm[1], pm[2], d, md, gqc, L.N, L.NG);
+        vc = qcorr_slot(T, B, x, y, z, d, md, gqc, L.N, L.NG);
+        vm = -qcorr_slot(T, B, pm[0], pm[1], pm[2], d, md, gqc, L.N, L.NG);
     } else if (m_out) {
-        vp = qcorr_slot(S, B, pp[0], pp[1], pp[2], d, md, gqc, L.N, L.NG);
-        vc = -qcorr_slot(S, B, x, y, z, d, md, gqc, L.N, L.NG);
+        vp = qcorr_slot(T, B, pp[0], pp[1], pp[2], d, md, gqc, L.N, L.NG);
+        vc = -qcorr_slot(T, B, x, y, z, d, md, gqc, L.N, L.NG);
         vm = 0.0;
     } else {
-        vp = 0.5 * qcorr_slot(S, B, pp[0], pp[1], pp[2], d, md, gqc, L.N, L.NG);
+        vp = 0.5 * qcorr_slot(T, B, pp[0], pp[1], pp[2], d, md, gqc, L.N, L.NG);
         vc = 0.0;
-        vm = -0.5 * qcorr_slot(S, B, pm[0], pm[1], pm[2], d, md, gqc, L.N, L.NG);
+        vm = -0.5 * qcorr_slot(T, B, pm[0], pm[1], pm[2], d, md, gqc, L.N, L.NG);
     }
     return (vp + vc + vm) * idx;
 }
 
-// the CTA's tile: its box's slot map in shared memory, the thread's cell
+// the CTA's tile: its box's slot table in shared memory, the thread's cell
 template <int MODE>
-__device__ __forceinline__ bool tile_setup(const LV& L, const LevelPlan& lp, const Tile* tiles, NbrSlot* sl, int& b,
-                                           int& x, int& y, int& z, long long& c)
+__device__ __forceinline__ bool tile_setup(const LV& L, const LevelPlan& lp, const Tile* tiles, NbrSlot* sl,
+                                           SlotTab& T, int& b, int& x, int& y, int& z, long long& c)
 {
     if (MODE > 0) {
         const int box = tiles[blockIdx.x].box;
-        if (threadIdx.x < 27) sl[threadIdx.x] = lp.slots[(long long)box * 27 + threadIdx.x];
+        const DevBox& B = L.box[box];
+        int tc[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            T.lg[d] = lp.slot_lg[d];
+            tc[d] = ((B.n[d] + (1 << T.lg[d]) - 1) >> T.lg[d]) + 2;
+            T.top[d] = tc[d] - 1;
+        }
+        T.tx = tc[0];
+        T.ty = tc[1];
+        T.s = sl;
+        const int n = tc[0] * tc[1] * tc[2];
+        const NbrSlot* src = lp.slots + lp.slot_off[box];
+        for (int i = threadIdx.x; i < n; i += blockDim.x) sl[i] = src[i];
         __syncthreads();
     }
     return cell_of_tile(L, tiles, b, x, y, z, c);
@@ -125,10 +153,11 @@ __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, LevelPlan lp, BCPa
                                                         const double* gAg, const double* fB, const double* gB,
                                                         double* md)
 {
-    __shared__ NbrSlot sl[27];
+    extern __shared__ NbrSlot sl[];
+    SlotTab T;
     int b, x, y, z;
     long long c;
-    if (!tile_setup<MODE>(L, lp, tiles, sl, b, x, y, z, c)) return;
+    if (!tile_setup<MODE>(L, lp, tiles, sl, T, b, x, y, z, c)) return;
     const DevBox& B = L.box[b];
     const uint8_t tf = flag_at(L, B, x, y, z);
     if (!(tf & FL_FLUID)) return;
@@ -136,11 +165,11 @@ __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, LevelPlan lp, BCPa
     const bool interior = !ovr && is_interior(B, x, y, z);
     const long long cell = B.voff + c;
     MomentAcc<double> acc;
-#define MBG_PULLF(q) (MODE == 1 ? pull_slot<q>(sl, B, x, y, z, fA, fAg, L.N, L.NG)                  \
-                     : MODE == 2 ? pull_slot_eb<q>(L, sl, B, x, y, z, fA, fAg)                       \
+#define MBG_PULLF(q) (MODE == 1 ? pull_slot<q>(T, B, x, y, z, fA, fAg, L.N, L.NG)                  \
+                     : MODE == 2 ? pull_slot_eb<q>(L, T, B, x, y, z, fA, fAg)                       \
                                  : pull<q>(L, P, B, x, y, z, tf, interior, fA, fAg, false, ph.lat))
-#define MBG_PULLG(q) (MODE == 1 ? pull_slot<q>(sl, B, x, y, z, gA, gAg, L.N, L.NG)                  \
-                     : MODE == 2 ? pull_slot_eb<q>(L, sl, B, x, y, z, gA, gAg)                       \
+#define MBG_PULLG(q) (MODE == 1 ? pull_slot<q>(T, B, x, y, z, gA, gAg, L.N, L.NG)                  \
+                     : MODE == 2 ? pull_slot_eb<q>(L, T, B, x, y, z, gA, gAg)                       \
                                  : pull<q>(L, P, B, x, y, z, tf, interior, gA, gAg, true, ph.lat))
 #define MBG_M64(q)                                                             \
     {                                                                          \
@@ -181,10 +210,11 @@ __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, LevelPlan lp, BCPa
                                                         const double* gAg, double* fB, double* gB,
                                                         const double* md, const double* gqc)
 {
-    __shared__ NbrSlot sl[27];
+    extern __shared__ NbrSlot sl[];
+    SlotTab T;
     int b, x, y, z;
     long long c;
-    if (!tile_setup<MODE>(L, lp, tiles, sl, b, x, y, z, c)) return;
+    if (!tile_setup<MODE>(L, lp, tiles, sl, T, b, x, y, z, c)) return;
     const DevBox& B = L.box[b];
     const uint8_t tf = flag_at(L, B, x, y, z);
     const long long N = L.N;
@@ -218,9 +248,9 @@ __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, LevelPlan lp, BCPa
     m.temp = md[MD_T * N + cell];
     double dqx, dqy, dqz;
     if (MODE > 0) {
-        dqx = qgrad_slot<MODE == 2>(L, sl, B, x, y, z, 0, ph.idx[0], md, gqc);
-        dqy = qgrad_slot<MODE == 2>(L, sl, B, x, y, z, 1, ph.idx[1], md, gqc);
-        dqz = qgrad_slot<MODE == 2>(L, sl, B, x, y, z, 2, ph.idx[2], md, gqc);
+        dqx = qgrad_slot<MODE == 2>(L, T, B, x, y, z, 0, ph.idx[0], md, gqc);
+        dqy = qgrad_slot<MODE == 2>(L, T, B, x, y, z, 1, ph.idx[1], md, gqc);
+        dqz = qgrad_slot<MODE == 2>(L, T, B, x, y, z, 2, ph.idx[2], md, gqc);
     } else {
         dqx = qgrad(L, B, x, y, z, 0, ph.idx[0], md, gqc);
         dqy = qgrad(L, B, x, y, z, 1, ph.idx[1], md, gqc);
@@ -252,35 +282,37 @@ __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, LevelPlan lp, BCPa
 }
 
 // ---- launchers -----------------------------------------------------------
-// the fast tiles through the slot maps, the others through the general pull
+static size_t slot_bytes(const LevelPlan& lp) { return (size_t)lp.slot_max * sizeof(NbrSlot); }
+
+// the slot-table tiles (all fluid, holding solids), then the others through
+// the general pull
 void launch_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
                     const double* fAg, const double* gAg, const double* fB, const double* gB, double* md,
                     cudaStream_t s)
 {
+    const size_t sb = slot_bytes(lp);
+    const LV& L = lp.view64;
     if (lp.nfast > 0)
-        k_moments<1><<<lp.nfast, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB, gB,
-                                                    md);
+        k_moments<1><<<lp.nfast, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB, gB, md);
     if (lp.nfasteb > 0)
-        k_moments<2><<<lp.nfasteb, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fasteb_tiles, fA, gA, fAg, gAg, fB,
-                                                      gB, md);
+        k_moments<2><<<lp.nfasteb, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fasteb_tiles, fA, gA, fAg, gAg, fB, gB, md);
     if (lp.ngen > 0)
-        k_moments<0><<<lp.ngen, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB, gB,
-                                                   md);
+        k_moments<0><<<lp.ngen, TILE_CELLS, 0, s>>>(L, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB, gB, md);
 }
 
 void launch_collide(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
                     const double* fAg, const double* gAg, double* fB, double* gB, const double* md,
                     const double* gqc, cudaStream_t s)
 {
+    const size_t sb = slot_bytes(lp);
+    const LV& L = lp.view64;
     if (lp.nfast > 0)
-        k_collide<1><<<lp.nfast, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB, gB,
-                                                    md, gqc);
+        k_collide<1><<<lp.nfast, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB, gB, md, gqc);
     if (lp.nfasteb > 0)
-        k_collide<2><<<lp.nfasteb, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.fasteb_tiles, fA, gA, fAg, gAg, fB,
-                                                      gB, md, gqc);
+        k_collide<2><<<lp.nfasteb, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fasteb_tiles, fA, gA, fAg, gAg, fB, gB, md,
+                                                        gqc);
     if (lp.ngen > 0)
-        k_collide<0><<<lp.ngen, TILE_CELLS, 0, s>>>(lp.view64, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB, gB,
-                                                   md, gqc);
+        k_collide<0><<<lp.ngen, TILE_CELLS, 0, s>>>(L, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB, gB, md, gqc);
 }
 
 int fp64_step_launches(const LevelPlan& lp) { return (lp.nfast > 0) + (lp.nfasteb > 0) + (lp.ngen > 0); }

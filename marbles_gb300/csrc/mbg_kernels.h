@@ -60,27 +60,36 @@ struct Phys32 {
     float inv_fscale, inv_gscale;
 };
 
-// One of the 27 neighbour regions of a box (index ox + 3 oy + 9 oz, o = 0
-// below, 1 inside, 2 above the box along each axis; 13 is the box itself):
-// the storage of the cells there as an affine map of box-local positions,
-// index = base + z sz + y sy + x, into the valid cells of the level (stride
-// N) or into the box's own ghost fab (stride NG).
+// One chunk of a box's neighbourhood.  Along each axis the box grown by one
+// cell is cut into the layer below the box (chunk 0), runs of 2^lg cells of
+// the box (chunks 1 .. nch) and the layer above (chunk nch + 1); a box's
+// table holds one slot per chunk triple, index cx + tx (cy + ty cz) with
+// t = nch + 2.  A slot gives the storage of its cells as an affine map of
+// box-local positions, index = base + z sz + y sy + x, into the valid cells
+// of the level (stride N) or into the box's own ghost fab (stride NG).  With
+// 2^lg the largest power of two (at most 32) dividing every box corner and
+// length of the level, each chunk lies in one box or in none, so AMR levels
+// of uneven boxes on a blocking factor get tables too.
 struct NbrSlot {
     long long base;
     int sy, sz;
     int ghost;
     int pad;
 };
+constexpr int SLOT_TABLE_MAX = 1024;   // slots of one box's table (24 KB of shared memory)
 
 struct LevelPlan {
     LevelView<double> view64;
     const Tile* tiles = nullptr;
     int ntiles = 0;
-    // FP64 form: the tiles of boxes whose 27 neighbour regions each map to one
+    // FP64 form: the tiles of boxes whose neighbour chunks each map to one
     // box (or to the box's ghost fab), with no solid cell in the grown box and
-    // no non-periodic domain side within one cell -- their pulls are the slot
-    // maps above -- and the tiles of the other boxes (general pull)
-    const NbrSlot* slots = nullptr;   // [box][27]
+    // no non-periodic domain side within one cell -- their pulls go through
+    // the slot tables above -- and the tiles of the other boxes (general pull)
+    const NbrSlot* slots = nullptr;      // the boxes' tables, one after another
+    const int* slot_off = nullptr;       // [box]: first slot of the box's table (-1: none)
+    int slot_lg[3] = {0, 0, 0};          // log2 of the chunk length along each axis
+    int slot_max = 0;                    // largest table of a box on the slot lists
     const Tile* fast_tiles = nullptr;
     int nfast = 0;
     const Tile* fasteb_tiles = nullptr;   // the same for boxes holding solid cells
