@@ -196,15 +196,21 @@ mbg_status mbg_timing(mbg_ctx* ctx, int k, const char** name, long long* launche
 /* ---- autotuner ----------------------------------------------------------------
  * No counterpart in the reference.  The 16-bit forms have several
  * implementations of the level step: variant 0 runs it in two passes (Q_corr,
- * then collision), variants 1-2 fuse it into one pass over runs of 4 or 8
- * planes per thread block, variant 3 is the two-pass step with the collision
- * pass limited to 80 registers (6 resident blocks per SM).  mbg_autotune times every variant `reps` times on
- * each level's current data and keeps the fastest per level; the state is not
+ * then collision) on two x-adjacent cells per thread with paired FP32
+ * arithmetic wherever the box allows (even x extent, fluid one cell out), one
+ * cell per thread elsewhere; variants 1-2 fuse it into one pass over runs of
+ * 4 or 8 planes per thread block; variant 3 is the two-pass step on one cell
+ * per thread with the collision pass limited to 80 registers (6 resident
+ * blocks per SM).  mbg_autotune times every variant `reps` times on each
+ * level's current data and keeps the fastest per level; the state is not
  * changed.  mbg_tuning reports a level's chosen variant and the mean time per
- * step of each variant in ms (0 where not timed).  FP64 contexts have one
- * variant; both calls succeed and report variant 0. */
+ * step of each variant in ms (0 where not timed).  mbg_set_variant makes a
+ * level (lev >= 0) or every level (lev = -1) run the given variant.  FP64
+ * contexts have one variant; the calls succeed, report variant 0 and accept
+ * only variant 0. */
 mbg_status mbg_autotune(mbg_ctx* ctx, int reps);
 mbg_status mbg_tuning(mbg_ctx* ctx, int lev, int* variant, double ms[4]);
+mbg_status mbg_set_variant(mbg_ctx* ctx, int lev, int variant);
 
 /* ---- batched independent domains -----------------------------------------
  * No counterpart in the reference, which runs one domain per process.  Many

@@ -28,7 +28,7 @@ EXPORTS = [
     "mbg_lbm_level_boxes", "mbg_lbm_level_flags", "mbg_lbm_write_plotfile", "mbg_lbm_last_error",
     "mbg_lbm_destroy", "mbg_lbm_write_checkpoint", "mbg_lbm_step_time", "mbg_tag_cells", "mbg_regrid", "mbg_lbm_regrid",
     "mbg_geometry_flags",
-    "mbg_get_derived", "mbg_conserved", "mbg_autotune", "mbg_tuning",
+    "mbg_get_derived", "mbg_conserved", "mbg_autotune", "mbg_tuning", "mbg_set_variant",
     "mbg_write_plotfile", "mbg_write_multifab", "mbg_read_multifab",
     "mbg_batch_create", "mbg_batch_cells", "mbg_batch_set_state", "mbg_batch_get_state", "mbg_batch_get_macro",
     "mbg_batch_step", "mbg_batch_autotune", "mbg_batch_tuning", "mbg_batch_synchronize", "mbg_batch_launch_count",
@@ -319,6 +319,10 @@ class Context:
     def autotune(self, reps=3):
         """Time the step variants of every level and keep the fastest (16-bit forms)."""
         self._check(self.L.mbg_autotune(self.h, reps), "mbg_autotune")
+
+    def set_variant(self, variant, lev=-1):
+        """Run step variant `variant` on level lev (every level for lev = -1)."""
+        self._check(self.L.mbg_set_variant(self.h, lev, variant), "mbg_set_variant")
 
     def tuning(self, lev):
         """(chosen variant, [ms per step of variants 0..3]) of level lev."""

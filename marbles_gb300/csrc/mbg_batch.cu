@@ -46,8 +46,12 @@ struct mbg_batch {
     double* tmp = nullptr;
     HaloCell* halo = nullptr;
     long long nhalo = 0;
-    Tile* tiles = nullptr;             // 128-cell tiles (two-pass variant, state transfer)
+    Tile* tiles = nullptr;             // 128-cell tiles (two-pass variant 3, state transfer)
     int ntiles = 0;
+    Tile* ptiles = nullptr;            // variant 0: pair tiles and per-cell tiles (step_tiles)
+    int nptiles = 0;
+    Tile* ctiles = nullptr;
+    int nctiles = 0;
     FusedTile* ftiles[2] = {nullptr, nullptr};
     int nftiles[2] = {0, 0};
     int fgrid = 0;                     // persistent grid of the fused variants
@@ -60,6 +64,7 @@ struct mbg_batch {
     double variant_ms[4] = {0, 0, 0, 0};
     cudaGraphExec_t graph = nullptr;
     long long launches = 0;
+    long long graph_launches = 0;      // kernel launches of one replay of the two-step graph
 };
 
 static mbg_status bfail(mbg_batch* b, mbg_status st, const std::string& m)
@@ -101,8 +106,11 @@ static void launch_step(mbg_batch* b, int cur)
     if (b->variant == 0 || b->variant == 3) {
         // no pad of Q_corr: every domain face is one-sided
         const QPtrs qp = make_qptrs(b->f[cur], b->g[cur], b->f[1 - cur], b->g[1 - cur], b->N);
-        LOWP16(b->bf, two_pass, k, b->ct, b->lat, b->tiles, b->ntiles, b->halo, 0, b->qs, qp, b->variant == 3, b->s);
-        b->launches += 4;
+        const bool pairs = b->variant == 0;
+        b->launches += 1 + LOWP16(b->bf, two_pass, k, b->ct, b->lat, pairs ? b->ctiles : b->tiles,
+                                  pairs ? b->nctiles : b->ntiles, b->ptiles, pairs ? b->nptiles : 0, nullptr, 0,
+                                  QPad{},
+                                  b->qs, qp, !pairs, b->s);
     } else {
         const int v = b->variant - 1;
         LOWP16(b->bf, fused, k, b->ct, b->lat, b->ftiles[v], b->nftiles[v], std::min(b->fgrid, b->nftiles[v]), b->s);
@@ -185,6 +193,10 @@ mbg_status mbg_batch_create(const mbg_params* common, int ndom, const mbg_domain
         for (long long s0 = 0; s0 < vol; s0 += TILE_CELLS) tiles.push_back(Tile{i, (int)s0});
     }
     b->ntiles = (int)tiles.size();
+    std::vector<Tile> ptiles, potiles, ctiles;
+    step_tiles(b->hbox, nullptr, ptiles, potiles, ctiles);
+    b->nptiles = (int)ptiles.size();
+    b->nctiles = (int)ctiles.size();
     mbg_status st = MBG_OK;
     // domains in decreasing size, so that the persistent grid's strided walk
     // through the work list takes the largest first
@@ -203,6 +215,8 @@ mbg_status mbg_batch_create(const mbg_params* common, int ndom, const mbg_domain
         if ((s2 = balloc(b, &b->d_phys, ndom)) != MBG_OK) return s2;
         if ((s2 = balloc(b, &b->halo, halo.size())) != MBG_OK) return s2;
         if ((s2 = balloc(b, &b->tiles, tiles.size())) != MBG_OK) return s2;
+        if ((s2 = balloc(b, &b->ptiles, ptiles.size())) != MBG_OK) return s2;
+        if ((s2 = balloc(b, &b->ctiles, ctiles.size())) != MBG_OK) return s2;
         for (int v = 0; v < 2; ++v) {
             std::vector<FusedTile> ft = fused_tiles(sorted, FUSED_ZC[v]);
             for (FusedTile& t : ft) t.box = order[t.box];
@@ -237,7 +251,11 @@ mbg_status mbg_batch_create(const mbg_params* common, int ndom, const mbg_domain
               cudaMemcpyAsync(b->halo, halo.data(), halo.size() * sizeof(HaloCell), cudaMemcpyHostToDevice, s) ==
                   cudaSuccess &&
               cudaMemcpyAsync(b->tiles, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, s) ==
-                  cudaSuccess;
+                  cudaSuccess &&
+              (ptiles.empty() || cudaMemcpyAsync(b->ptiles, ptiles.data(), ptiles.size() * sizeof(Tile),
+                                                 cudaMemcpyHostToDevice, s) == cudaSuccess) &&
+              (ctiles.empty() || cudaMemcpyAsync(b->ctiles, ctiles.data(), ctiles.size() * sizeof(Tile),
+                                                 cudaMemcpyHostToDevice, s) == cudaSuccess);
     for (int i = 0; i < 2 && ok; ++i)
         ok = cudaMemsetAsync(b->f[i], 0xFF, (size_t)b->N * NQ * 2, s) == cudaSuccess &&
              cudaMemsetAsync(b->g[i], 0xFF, (size_t)b->N * NQ * 2, s) == cudaSuccess;
@@ -362,6 +380,7 @@ mbg_status mbg_batch_step(mbg_batch* b, int nsteps)
         const long long l0 = b->launches;
         launch_step(b, 0);
         launch_step(b, 1);
+        b->graph_launches = b->launches - l0;
         b->launches = l0;
         cudaError_t e = cudaStreamEndCapture(b->s, &gr);
         if (e != cudaSuccess) return bfail(b, MBG_ECUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
@@ -375,7 +394,7 @@ mbg_status mbg_batch_step(mbg_batch* b, int nsteps)
     while (left > 0) {
         if (left >= 2 && b->graph && b->cur == 0) {
             BCUDA(cudaGraphLaunch(b->graph, b->s));
-            b->launches += b->variant == 0 ? 8 : 4;
+            b->launches += b->graph_launches;
             left -= 2;
         } else {
             launch_step(b, b->cur);

@@ -727,6 +727,7 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
         }
         // re-upload the coarse flags with the coalescence bits
         MBG_CUDA(cudaMemcpyAsync(C.d_flags, C.hflags.data(), C.hflags.size(), cudaMemcpyHostToDevice, ctx->s));
+        if (p.precision != MBG_FP64) lowp_retile(C.lowp, C.hflags, ctx->s);
     }
     // device allocations
     mbg_status st;
@@ -1135,6 +1136,19 @@ mbg_status mbg_tuning(mbg_ctx* ctx, int lev, int* variant, double ms[4])
     return MBG_OK;
 }
 
+mbg_status mbg_set_variant(mbg_ctx* ctx, int lev, int variant)
+{
+    if (!ctx) return MBG_EINVAL;
+    drop_graph(ctx);
+    if (lev < -1 || lev >= (int)ctx->lv.size()) return fail(ctx, MBG_EINVAL, "mbg_set_variant: no such level");
+    const int nv = ctx->p.precision == MBG_FP64 ? 1 : lowp_variants();
+    if (variant < 0 || variant >= nv) return fail(ctx, MBG_EINVAL, "mbg_set_variant: no such variant");
+    if (ctx->p.precision == MBG_FP64) return MBG_OK;
+    for (int l = 0; l < (int)ctx->lv.size(); ++l)
+        if (lev < 0 || l == lev) lowp_set_variant(ctx->lv[l].lowp, variant);
+    return MBG_OK;
+}
+
 mbg_status mbg_average_down(mbg_ctx* ctx, int crse_lev, int crse_ng)
 {
     if (!ctx) return MBG_EINVAL;
@@ -1278,6 +1292,7 @@ static mbg_status drop_levels(mbg_ctx* ctx, int first)
     C.ncoal1 = C.ncoal0 = 0;
     for (auto& v : C.hflags) v = (uint8_t)(v & ~(FL_OVR | FL_COV));
     MBG_CUDA(cudaMemcpyAsync(C.d_flags, C.hflags.data(), C.hflags.size(), cudaMemcpyHostToDevice, ctx->s));
+    if (ctx->p.precision != MBG_FP64) lowp_retile(C.lowp, C.hflags, ctx->s);
     MBG_CUDA(cudaStreamSynchronize(ctx->s));
     return MBG_OK;
 }

@@ -31,6 +31,14 @@ struct LowpDev {
     int variant = 0;
     double variant_ms[4] = {0, 0, 0, 0};   // tuner's timings (0: not timed)
     float* qs = nullptr;         // Q_corr of the two-pass step, [3][N]
+    QPad qpad;                   // Q_corr of the pad (qpad_plan)
+    Tile* ptiles = nullptr;      // variant 0: pair tiles without / with overwritten cells, per-cell
+    int nptiles = 0;             // tiles (step_tiles); the pair lists hold room for every pair tile
+    Tile* potiles = nullptr;
+    int nootiles = 0;
+    Tile* ctiles = nullptr;
+    int nctiles = 0;
+    std::vector<DevBox> box16h;  // host copy of box16
     HaloCell* halo = nullptr;    // every pad cell of every box
     long long* gdst = nullptr;   // pad fill by gather: destination and source indices
     long long* gsrc = nullptr;
@@ -145,10 +153,54 @@ long long pad_boxes(std::vector<DevBox>& box)
         const long long px = B.n[0] + 2, py = B.n[1] + 2, pz = B.n[2] + 2;
         B.sy = (int)px;
         B.sz = (int)(px * py);
+        // valid cell (0,0,0) at an even index, so that the cell pairs (x even)
+        // of a box with an even x extent are 4-byte aligned
+        if ((np + B.sz + B.sy + 1) & 1) ++np;
         B.voff = np + B.sz + B.sy + 1;
         np += px * py * pz;
     }
-    return np;
+    // an even component stride keeps that alignment in every component
+    return np + (np & 1);
+}
+
+void step_tiles(const std::vector<DevBox>& box, const std::vector<uint8_t>* flags, std::vector<Tile>& pair,
+                std::vector<Tile>& pair_ovr, std::vector<Tile>& cell)
+{
+    pair.clear();
+    pair_ovr.clear();
+    cell.clear();
+    for (size_t n = 0; n < box.size(); ++n) {
+        const DevBox& B = box[n];
+        const long long vol = (long long)B.n[0] * B.n[1] * B.n[2];
+        if (B.n[0] % 2 == 0 && B.vfluid && B.voff % 2 == 0) {
+            for (long long s = 0; s < vol; s += PAIR_CELLS) {
+                bool ovr = false;
+                for (long long c = s; c < std::min(vol, s + PAIR_CELLS) && flags && !ovr; ++c) {
+                    const int x = (int)(c % B.n[0]), y = (int)((c / B.n[0]) % B.n[1]), z = (int)(c / B.n[0] / B.n[1]);
+                    const long long fi = B.foff + ((long long)(z + 3) * (B.n[1] + 6) + (y + 3)) * (B.n[0] + 6) + (x + 3);
+                    ovr = (*flags)[fi] & FL_OVR;
+                }
+                (ovr ? pair_ovr : pair).push_back(Tile{(int)n, (int)s});
+            }
+        } else {
+            for (long long s = 0; s < vol; s += TILE_CELLS) cell.push_back(Tile{(int)n, (int)s});
+        }
+    }
+}
+
+// the pair tile lists again after the level's flags gained or lost cells
+// overwritten by coalescence (a finer level defined or dropped)
+void lowp_retile(LowpLevel& L, const std::vector<uint8_t>& flags, cudaStream_t s)
+{
+    LowpDev* D = dev_of(L);
+    if (!D) return;
+    std::vector<Tile> pt, po, ctl;
+    step_tiles(D->box16h, &flags, pt, po, ctl);
+    D->nptiles = (int)pt.size();
+    D->nootiles = (int)po.size();
+    if (!pt.empty()) cudaMemcpyAsync(D->ptiles, pt.data(), pt.size() * sizeof(Tile), cudaMemcpyHostToDevice, s);
+    if (!po.empty()) cudaMemcpyAsync(D->potiles, po.data(), po.size() * sizeof(Tile), cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);   // the host vectors end here
 }
 
 // every pad cell of every box, faces first, then edges, then corners, so that
@@ -192,6 +244,41 @@ std::vector<FusedTile> fused_tiles(const std::vector<DevBox>& box, int zc)
                                               (short)std::min(box[n].n[2], z0 + zc), (short)lgw, 0});
     }
     return tiles;
+}
+
+// Q_corr pad plan: the face cells of every box's pad inside the domain box
+// that hold fluid (edges and corners are on no gradient stencil, cells
+// outside the domain box are read by no one-sided gradient, solid ones by
+// no gradient at all; their zeros from set-up stay), each a copy from the
+// owning box's valid cell or, on the coarse-fine shell, a ghost entry.
+static void qpad_plan(const std::vector<DevBox>& box, const std::vector<HaloCell>& halo, long long N,
+                      const LevelHost& h, std::vector<long long>& dst, std::vector<long long>& src,
+                      std::vector<HaloCell>& ghost)
+{
+    auto fab = [](const DevBox& B, int x, int y, int z) {
+        return ((long long)(z + 3) * (B.n[1] + 6) + (y + 3)) * (B.n[0] + 6) + (x + 3);
+    };
+    const std::vector<uint8_t>& fl = *h.flags;
+    for (const HaloCell& c : halo) {
+        const DevBox& B = box[c.box];
+        const int out0 = c.x < 0 || c.x >= B.n[0], out1 = c.y < 0 || c.y >= B.n[1], out2 = c.z < 0 || c.z >= B.n[2];
+        if (out0 + out1 + out2 != 1) continue;
+        const int d = out0 ? 0 : out1 ? 1 : 2;
+        const int gp[3] = {B.lo[0] + c.x, B.lo[1] + c.y, B.lo[2] + c.z};
+        bool inside = true;
+        for (int a = 0; a < 3; ++a) inside = inside && gp[a] >= h.dlo[a] && gp[a] <= h.dhi[a];
+        if (!inside || !(fl[B.foff + fab(B, c.x, c.y, c.z)] & FL_FLUID)) continue;
+        const int bi = (gp[0] - h.dlo[0]) / h.G[0], bj = (gp[1] - h.dlo[1]) / h.G[1], bk = (gp[2] - h.dlo[2]) / h.G[2];
+        const int o = (*h.omap)[((size_t)bk * h.nb[1] + bj) * h.nb[0] + bi];
+        if (o >= 0) {
+            const DevBox& O = box[o];
+            dst.push_back((long long)d * N + B.voff + (long long)c.z * B.sz + (long long)c.y * B.sy + c.x);
+            src.push_back((long long)d * N + O.voff + (long long)(gp[2] - O.lo[2]) * O.sz +
+                          (long long)(gp[1] - O.lo[1]) * O.sy + (gp[0] - O.lo[0]));
+        } else if (B.goff >= 0) {
+            ghost.push_back(c);
+        }
+    }
 }
 
 // Pad fill plan: for every (pad cell, inward direction) whose target is a
@@ -389,6 +476,9 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     if (host.ghosts && NG > 0) ghost_plan(box, *host.ghosts, L.N, NG, host, sdst, ssrc, scell, sq);
     sort_plan(sdst, ssrc);
     D->nhalo = (long long)halo.size();
+    std::vector<long long> qdst, qsrc;
+    std::vector<HaloCell> qghost;
+    qpad_plan(box, halo, L.N, host, qdst, qsrc, qghost);
     mbg_status st;
     if ((st = lalloc(L, (void**)&D->box16, box.size() * sizeof(DevBox), err)) != MBG_OK) return st;
     for (int v = 0; v < 2; ++v) {
@@ -396,6 +486,37 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
         D->nftiles[v] = (int)tiles.size();
         if ((st = lalloc(L, (void**)&D->ftiles[v], tiles.size() * sizeof(FusedTile), err)) != MBG_OK) return st;
         cudaMemcpy(D->ftiles[v], tiles.data(), tiles.size() * sizeof(FusedTile), cudaMemcpyHostToDevice);
+    }
+    {
+        std::vector<Tile> pt, po, ctl;
+        step_tiles(box, host.flags, pt, po, ctl);
+        D->nptiles = (int)pt.size();
+        D->nootiles = (int)po.size();
+        D->nctiles = (int)ctl.size();
+        const size_t cap = pt.size() + po.size();
+        if ((st = lalloc(L, (void**)&D->ptiles, cap * sizeof(Tile), err)) != MBG_OK) return st;
+        if ((st = lalloc(L, (void**)&D->potiles, cap * sizeof(Tile), err)) != MBG_OK) return st;
+        if ((st = lalloc(L, (void**)&D->ctiles, ctl.size() * sizeof(Tile), err)) != MBG_OK) return st;
+        cudaMemcpy(D->ptiles, pt.data(), pt.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+        cudaMemcpy(D->potiles, po.data(), po.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+        cudaMemcpy(D->ctiles, ctl.data(), ctl.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+        D->box16h = box;
+    }
+    {
+        long long* qd = nullptr;
+        long long* qsr = nullptr;
+        HaloCell* qg = nullptr;
+        if ((st = lalloc(L, (void**)&qd, qdst.size() * sizeof(long long), err)) != MBG_OK) return st;
+        if ((st = lalloc(L, (void**)&qsr, qsrc.size() * sizeof(long long), err)) != MBG_OK) return st;
+        if ((st = lalloc(L, (void**)&qg, qghost.size() * sizeof(HaloCell), err)) != MBG_OK) return st;
+        cudaMemcpy(qd, qdst.data(), qdst.size() * sizeof(long long), cudaMemcpyHostToDevice);
+        cudaMemcpy(qsr, qsrc.data(), qsrc.size() * sizeof(long long), cudaMemcpyHostToDevice);
+        cudaMemcpy(qg, qghost.data(), qghost.size() * sizeof(HaloCell), cudaMemcpyHostToDevice);
+        D->qpad.dst = qd;
+        D->qpad.src = qsr;
+        D->qpad.ncopy = (long long)qdst.size();
+        D->qpad.ghost = qg;
+        D->qpad.nghost = (long long)qghost.size();
     }
     if ((st = lalloc(L, (void**)&D->halo, halo.size() * sizeof(HaloCell), err)) != MBG_OK) return st;
     D->ngather = (long long)gdst.size();
@@ -628,14 +749,15 @@ int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const Le
         ++launches;
     }
     if (D->variant == 0 || D->variant == 3) {
-        const int tight = D->variant == 3;
+        const bool pairs = D->variant == 0;
+        const Tile* ct = pairs ? D->ctiles : plan.tiles;
+        const int nct = pairs ? D->nctiles : plan.ntiles;
         run(LOWP_STAGE_FUSED,
             [&] {
                 const QPtrs qp = make_qptrs(L.f[A], L.g[A], L.f[1 - A], L.g[1 - A], L.N);
-                LOWP16(bf, two_pass, k, D->ct, D->lat, plan.tiles, plan.ntiles, D->halo, D->nhalo, D->qs, qp, tight,
-                       s);
+                launches += LOWP16(bf, two_pass, k, D->ct, D->lat, ct, nct, D->ptiles, pairs ? D->nptiles : 0,
+                                   D->potiles, pairs ? D->nootiles : 0, D->qpad, D->qs, qp, !pairs, s);
             });
-        launches += 3;
     } else {
         const int v = D->variant - 1;
         run(LOWP_STAGE_FUSED,
@@ -698,6 +820,8 @@ mbg_status lowp_autotune(LowpLevel& L, const LevelPlan& plan, const BCParams& bc
     cudaEventDestroy(b);
     return MBG_OK;
 }
+
+void lowp_set_variant(LowpLevel& L, int variant) { dev_of(L)->variant = variant; }
 
 void lowp_variant(LowpLevel& L, int* variant, double ms[4])
 {

@@ -43,6 +43,8 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
                        long long NG, double dt, const double idx[3], const LevelHost& host, LowpLevel& L,
                        std::string& err);
 void lowp_release(LowpLevel& L);
+// rebuild the step's tile lists after the level's FL_OVR flags changed
+void lowp_retile(LowpLevel& L, const std::vector<uint8_t>& flags, cudaStream_t s);
 mbg_status lowp_set_state(LowpLevel& L, const LevelPlan& plan, const std::vector<DevBox>& hbox, const double* f,
                           const double* g, cudaStream_t s, std::string& err);
 mbg_status lowp_get_state(LowpLevel& L, const LevelPlan& plan, const std::vector<DevBox>& hbox, double* f,
@@ -71,6 +73,7 @@ mbg_status lowp_autotune(LowpLevel& L, const LevelPlan& plan, const BCParams& bc
                          long long ncoal, const LowpLevel* fine, const LevelPlan* fplan, int reps, cudaStream_t s,
                          std::string& err);
 void lowp_variant(LowpLevel& L, int* variant, double ms[4]);
+void lowp_set_variant(LowpLevel& L, int variant);
 // returns the number of kernels launched
 int lowp_explode(LowpLevel& F, const LevelPlan& fplan, const LowpLevel& C, const LevelPlan& cplan, cudaStream_t s);
 void lowp_average_down(LowpLevel& C, const LevelPlan& cplan, const LowpLevel& F, const LevelPlan& fplan,

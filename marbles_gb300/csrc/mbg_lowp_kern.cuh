@@ -36,6 +36,7 @@
 #include <cuda_fp16.h>
 
 #include "mbg_lowp_types.cuh"
+#include "mbg_pair.cuh"
 
 namespace mbg {
 
@@ -692,6 +693,319 @@ __global__ void __launch_bounds__(TILE_CELLS, MINB)
     }
 }
 
+// ---- the two-pass step on cell pairs ----------------------------------------
+// Boxes with an even x extent whose cells one layer out are all fluid run
+// the same two passes on two x-adjacent cells per thread (x even): the
+// codes of a direction are one 32-bit word per lattice where the source
+// pair is aligned (directions with ex = 0) and two 16-bit loads otherwise,
+// the collision pulls again for the relaxation (L1 hits, so that the 54 code
+// pairs need no registers across the equilibria), and the moments, equilibria,
+// relaxation and encoding of both cells run as paired FP32 instructions
+// (mbg_pair.cuh).  The new codes of a direction go out as one aligned
+// 32-bit store per lattice.  Pulls of fluid targets in such boxes never
+// meet the stream sentinel, and the outputs of fluid cells are encoded
+// without the -1 test; a NaN encodes to the canonical NaN code (0x7FFF in
+// both formats), never to a sentinel.
+
+// codec constants per direction, each broadcast to both lanes
+struct CodecPair {
+    float2 frest[NQ], grest[NQ], fsc[NQ], gsc[NQ], fisc[NQ], gisc[NQ];
+};
+
+inline CodecPair make_codec_pair(const CodecTab& ct)
+{
+    CodecPair c;
+    for (int q = 0; q < NQ; ++q) {
+        c.frest[q] = make_float2(ct.frest[q], ct.frest[q]);
+        c.grest[q] = make_float2(ct.grest[q], ct.grest[q]);
+        c.fsc[q] = make_float2(ct.fsc[q], ct.fsc[q]);
+        c.gsc[q] = make_float2(ct.gsc[q], ct.gsc[q]);
+        c.fisc[q] = make_float2(ct.fisc[q], ct.fisc[q]);
+        c.gisc[q] = make_float2(ct.gisc[q], ct.gisc[q]);
+    }
+    return c;
+}
+
+// the two 16-bit codes of a word (low half: cell x) as FP32
+template <bool BF>
+__device__ __forceinline__ float2 h2f_pair(unsigned w)
+{
+    if constexpr (BF) {
+        return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xFFFF0000u));
+    } else {
+        __half2_raw r;
+        r.x = (unsigned short)(w & 0xFFFFu);
+        r.y = (unsigned short)(w >> 16);
+        return __half22float2(__half2(r));
+    }
+}
+
+template <bool BF>
+__device__ __forceinline__ unsigned f2h_pair(float2 v)
+{
+    if constexpr (BF) {
+        const __nv_bfloat162_raw r = __float22bfloat162_rn(v);
+        return (unsigned)r.x | ((unsigned)r.y << 16);
+    } else {
+        const __half2_raw r = __float22half2_rn(v);
+        return (unsigned)r.x | ((unsigned)r.y << 16);
+    }
+}
+
+// read-only loads the compiler neither merges with the first pull's loads
+// of the same values (which would hold all 54 code pairs in registers across
+// the equilibria) nor drops
+__device__ __forceinline__ unsigned ld_pin32(const void* p)
+{
+    unsigned r;
+    asm volatile("ld.global.nc.b32 %0, [%1];" : "=r"(r) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ unsigned ld_pin16(const void* p)
+{
+    unsigned short r;
+    asm volatile("ld.global.nc.b16 %0, [%1];" : "=h"(r) : "l"(p));
+    return r;
+}
+
+// codes of direction q pulled to the target pair at storage index c (even)
+template <int q, bool PIN = false>
+__device__ __forceinline__ unsigned ld_pair(const u16* __restrict__ base, int c, int sy, int sz)
+{
+    constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
+    const u16* p = base + (c - (ez * sz + ey * sy + ex));
+    if constexpr (ex == 0) {
+        return PIN ? ld_pin32(p) : __ldg(reinterpret_cast<const unsigned*>(p));
+    } else {
+        const unsigned lo = PIN ? ld_pin16(p) : __ldg(p), hi = PIN ? ld_pin16(p + 1) : __ldg(p + 1);
+        return lo | (hi << 16);
+    }
+}
+
+// box-local cell pair of thread threadIdx.x of a pair tile (256 cells)
+__device__ __forceinline__ bool pair_cell(const DevBox& B, const Tile& t, int& x, int& y, int& z)
+{
+    const unsigned ci = (unsigned)t.start + 2u * threadIdx.x;
+    const unsigned nxy = (unsigned)B.n[0] * (unsigned)B.n[1];
+    if (ci >= nxy * (unsigned)B.n[2]) return false;
+    z = (int)(ci / nxy);
+    const unsigned r = ci - (unsigned)z * nxy;
+    y = (int)(r / (unsigned)B.n[0]);
+    x = (int)(r - (unsigned)y * (unsigned)B.n[0]);
+    return true;
+}
+
+// coalescence overrides of a cell pair: o0 / o1 when cell x / x + 1 is
+// overwritten (FL_OVR on a level with override buffers)
+struct PairOvr {
+    bool any, o0, o1;
+};
+
+template <bool BF>
+__device__ __forceinline__ PairOvr pair_ovr(const LowpK* __restrict__ K, const DevBox& B, int x, int y, int z)
+{
+    PairOvr o{false, false, false};
+    if (K->s.fo) {
+        o.o0 = flag_at(K->L, B, x, y, z) & FL_OVR;
+        o.o1 = flag_at(K->L, B, x + 1, y, z) & FL_OVR;
+        o.any = o.o0 || o.o1;
+    }
+    return o;
+}
+
+// pass 1: the pulled code pair of direction q of one lattice (v: its
+// source, ov: its override buffer); an overwritten cell takes the override
+// code where it is not NOOVR16.  Pairs with an overwritten cell store the
+// merged pair back into the override buffer (idempotent: a merged code is
+// never NOOVR16), so that pass 2 reads one word there instead of merging.
+template <int q>
+__device__ __forceinline__ unsigned code_merge(const u16* __restrict__ v, u16* __restrict__ ov, long long N,
+                                               const PairOvr& o, int c, int sy, int sz)
+{
+    unsigned r = ld_pair<q>(v, c, sy, sz);
+    if (o.any) {
+        unsigned* w = reinterpret_cast<unsigned*>(ov + q * N + c);
+        const unsigned ow = *w;
+        unsigned m = 0u;
+        if (o.o0 && (ow & 0xFFFFu) != NOOVR16) m |= 0x0000FFFFu;
+        if (o.o1 && (ow >> 16) != NOOVR16) m |= 0xFFFF0000u;
+        r = (ow & m) | (r & ~m);
+        *w = r;
+    }
+    return r;
+}
+
+// pass 2: the code pair of direction q, from the override buffer for pairs
+// with an overwritten cell (merged there by pass 1), else pulled
+template <int q, bool PIN>
+__device__ __forceinline__ unsigned code_sel(const u16* __restrict__ v, const u16* __restrict__ ov, long long N,
+                                             bool any, int c, int sy, int sz)
+{
+    constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
+    const u16* p = any ? ov + q * N + c : v + (c - (ez * sz + ey * sy + ex));
+    if constexpr (ex == 0) {
+        return PIN ? ld_pin32(p) : __ldg(reinterpret_cast<const unsigned*>(p));
+    } else {
+        const unsigned lo = PIN ? ld_pin16(p) : __ldg(p), hi = PIN ? ld_pin16(p + 1) : __ldg(p + 1);
+        return lo | (hi << 16);
+    }
+}
+
+template <bool BF, int q>
+__device__ __forceinline__ F2 dec_pair(unsigned w, float2 sc, float2 rest)
+{
+    return fma2(F2(h2f_pair<BF>(w)), F2(sc), F2(rest));
+}
+
+// moments of a pair: MERGE for pass 1, else the pass-2 selection
+template <bool BF, bool MERGE, bool OVR = false>
+__device__ __forceinline__ MomentAcc<F2> moments_pair(const LowpK* __restrict__ K, const CodecPair& cp,
+                                                      const QPtrs& qp, const PairOvr& o, int c, int sy, int sz)
+{
+    u16* __restrict__ fo = const_cast<u16*>(K->s.fo);
+    u16* __restrict__ go = const_cast<u16*>(K->s.go);
+    const long long N = K->L.N;
+    // all 54 code pairs first (54 loads in flight per thread), then the sums
+    unsigned wf[NQ], wg[NQ];
+    static_for<0, NQ>([&](auto Q) {
+        constexpr int q = Q.value;
+        if constexpr (MERGE) {
+            wf[q] = code_merge<q>(qp.f[q], fo, N, o, c, sy, sz);
+            wg[q] = code_merge<q>(qp.g[q], go, N, o, c, sy, sz);
+        } else {
+            wf[q] = code_sel<q, false>(qp.f[q], fo, N, OVR, c, sy, sz);
+            wg[q] = code_sel<q, false>(qp.g[q], go, N, OVR, c, sy, sz);
+        }
+    });
+    MomentAcc<F2> acc;
+    static_for<0, NQ>([&](auto Q) {
+        constexpr int q = Q.value;
+        acc.template add<q>(dec_pair<BF, q>(wf[q], cp.fsc[q], cp.frest[q]),
+                            dec_pair<BF, q>(wg[q], cp.gsc[q], cp.grest[q]));
+    });
+    return acc;
+}
+
+// pass 1 on pairs: Q_corr of both cells into qs (one aligned 8-byte store
+// per component)
+// OVR: a tile holding cells overwritten by coalescence (the others never
+// look at flags or override buffers)
+template <bool BF, bool OVR>
+__global__ void __launch_bounds__(TILE_CELLS) k_qcorr16p(const LowpK* __restrict__ K, const CodecPair cp,
+                                                         const Tile* __restrict__ tiles, float* __restrict__ qs,
+                                                         const QPtrs qp)
+{
+    const LV16& L = K->L;
+    const Tile t = tiles[blockIdx.x];
+    const DevBox& B = L.box[t.box];
+    int x, y, z;
+    if (!pair_cell(B, t, x, y, z)) return;
+    const int c = (int)(B.voff + val_lin(B, x, y, z));
+    const PairOvr o = OVR ? pair_ovr<BF>(K, B, x, y, z) : PairOvr{false, false, false};
+    const Macro<F2> m =
+        moments_pair<BF, true>(K, cp, qp, o, c, B.sy, B.sz).finish(F2(K->ph.mesh_speed), F2(K->ph.Rg), F2(K->ph.cv));
+    const long long N = L.N;
+    *reinterpret_cast<float2*>(qs + c) = m.qcx.v;
+    *reinterpret_cast<float2*>(qs + N + c) = m.qcy.v;
+    *reinterpret_cast<float2*>(qs + 2 * N + c) = m.qcz.v;
+}
+
+// relaxation and encoding of the three directions (ex, ey, -1 .. 1) of a
+// cell pair: f_eq = rf[ex][ey] phz[ez] (Equilibrium::feq); g_eq of
+// Equilibrium::geq regrouped as w_q (b + A4[ez^2] / 2 + ez cz) with b and cz
+// shared by the three, so that few partial sums are live at a time
+template <bool BF, int ex, int ey, bool OVR>
+__device__ __forceinline__ void relax_group(const LowpK* __restrict__ K, const CodecPair& cp,
+                                            const Lattice<float>& lat, const QPtrs& qp, const PairOvr& o,
+                                            const Equilibrium<F2>& E, F2 omega, F2 h0, F2 h1, int c, int sy, int sz)
+{
+    const F2 half(0.5f);
+    F2 s2 = E.A1[ex * ex] + E.A2[ey * ey];
+    if constexpr (ex * ey == 1) s2 = s2 + E.t3; else if constexpr (ex * ey == -1) s2 = s2 - E.t3;
+    F2 b = E.grho;
+    if constexpr (ex == 1) b = b + E.a1[0]; else if constexpr (ex == -1) b = b - E.a1[0];
+    if constexpr (ey == 1) b = b + E.a1[1]; else if constexpr (ey == -1) b = b - E.a1[1];
+    b = fma2(half, s2, b);
+    F2 cz = E.a1[2];
+    if constexpr (ex == 1) cz = fma2(half, E.t5, cz); else if constexpr (ex == -1) cz = cz - half * E.t5;
+    if constexpr (ey == 1) cz = fma2(half, E.t6, cz); else if constexpr (ey == -1) cz = cz - half * E.t6;
+    const F2 b1 = b + h1;
+    const u16* __restrict__ fo = K->s.fo;
+    const u16* __restrict__ go = K->s.go;
+    const long long N = K->L.N;
+    static_for<0, 3>([&](auto Z) {
+        constexpr int ez = Z.value - 1;
+        constexpr int q = find_dir(ex, ey, ez);
+        const F2 fq = dec_pair<BF, q>(code_sel<q, true>(qp.f[q], fo, N, OVR, c, sy, sz), cp.fsc[q], cp.frest[q]);
+        const F2 fn = fma2(omega, E.rf[ex + 1][ey + 1] * E.phz[ez + 1] - fq, fq);
+        *reinterpret_cast<unsigned*>(qp.fo[q] + c) = f2h_pair<BF>(((fn - F2(cp.frest[q])) * F2(cp.fisc[q])).v);
+        const F2 gsum = ez == 0 ? b + h0 : (ez == 1 ? b1 + cz : b1 - cz);
+        const F2 geq = gsum * F2(lat.w[q]);
+        const F2 gq = dec_pair<BF, q>(code_sel<q, true>(qp.g[q], go, N, OVR, c, sy, sz), cp.gsc[q], cp.grest[q]);
+        const F2 gn = fma2(omega, geq - gq, gq);
+        *reinterpret_cast<unsigned*>(qp.go[q] + c) = f2h_pair<BF>(((gn - F2(cp.grest[q])) * F2(cp.gisc[q])).v);
+    });
+}
+
+// pass 2 on pairs: moments again from the same codes, q-correction
+// gradient, equilibria, relaxation, encoding (OVR: a pair with a cell
+// overwritten by coalescence, its codes read from the override buffers)
+template <bool BF, bool OVR>
+__device__ __forceinline__ void collide_pair(const LowpK* __restrict__ K, const CodecPair& cp,
+                                             const Lattice<float>& lat, const float* __restrict__ qs, const QPtrs& qp,
+                                             const DevBox& B, const PairOvr& o, int x, int y, int z, int c)
+{
+    const LV16& L = K->L;
+    const int sy = B.sy, sz = B.sz;
+    const Phys32* __restrict__ PH = K->phys ? K->phys + B.phys : &K->ph;
+    const float Rg = K->ph.Rg, cv = K->ph.cv;
+    const Macro<F2> m =
+        moments_pair<BF, false, OVR>(K, cp, qp, o, c, sy, sz).finish(F2(K->ph.mesh_speed), F2(Rg), F2(cv));
+    // gradient() of Source/Utilities.H:279-312: the x neighbours inside the
+    // pair are the other cell's own value
+    const long long N = L.N;
+    const float xm = qs[c - 1], xp = qs[c + 2];
+    const float2 ym = *reinterpret_cast<const float2*>(qs + N + c - sy);
+    const float2 yp = *reinterpret_cast<const float2*>(qs + N + c + sy);
+    const float2 zm = *reinterpret_cast<const float2*>(qs + 2 * N + c - sz);
+    const float2 zp = *reinterpret_cast<const float2*>(qs + 2 * N + c + sz);
+    const bool px0 = present_vf(L, B, x, 0, 1), mx0 = present_vf(L, B, x, 0, -1);
+    const bool px1 = present_vf(L, B, x + 1, 0, 1), mx1 = present_vf(L, B, x + 1, 0, -1);
+    const bool py = present_vf(L, B, y, 1, 1), my = present_vf(L, B, y, 1, -1);
+    const bool pz = present_vf(L, B, z, 2, 1), mz = present_vf(L, B, z, 2, -1);
+    const float ix = PH->idx[0], iy = PH->idx[1], iz = PH->idx[2];
+    const F2 dqx(grad1(px0, mx0, m.qcx.v.y, m.qcx.v.x, xm, ix), grad1(px1, mx1, xp, m.qcx.v.y, m.qcx.v.x, ix));
+    const F2 dqy(grad1(py, my, yp.x, m.qcy.v.x, ym.x, iy), grad1(py, my, yp.y, m.qcy.v.y, ym.y, iy));
+    const F2 dqz(grad1(pz, mz, zp.x, m.qcz.v.x, zm.x, iz), grad1(pz, mz, zp.y, m.qcz.v.y, zm.y, iz));
+    Equilibrium<F2> E;
+    const F2 omega = build_equilibrium<F2>(m, dqx, dqy, dqz, F2(PH->nu), F2(PH->alpha), F2(PH->dt), F2(Rg), F2(cv),
+                                           lat, E);
+    const F2 h0 = F2(0.5f) * E.A4[0], h1 = F2(0.5f) * E.A4[1];
+    static_for<0, 9>([&](auto G) {
+        relax_group<BF, G.value % 3 - 1, G.value / 3 - 1, OVR>(K, cp, lat, qp, o, E, omega, h0, h1, c, sy, sz);
+    });
+}
+
+template <bool BF, bool OVR>
+__global__ void __launch_bounds__(TILE_CELLS, 4) k_collide16p(const LowpK* __restrict__ K, const CodecPair cp,
+                                                           const Lattice<float> lat, const Tile* __restrict__ tiles,
+                                                           const float* __restrict__ qs, const QPtrs qp)
+{
+    const LV16& L = K->L;
+    const Tile t = tiles[blockIdx.x];
+    const DevBox& B = L.box[t.box];
+    int x, y, z;
+    if (!pair_cell(B, t, x, y, z)) return;
+    const int c = (int)(B.voff + val_lin(B, x, y, z));
+    if constexpr (OVR) {
+        const PairOvr o = pair_ovr<BF>(K, B, x, y, z);
+        if (o.any) collide_pair<BF, true>(K, cp, lat, qs, qp, B, o, x, y, z, c);
+        else collide_pair<BF, false>(K, cp, lat, qs, qp, B, o, x, y, z, c);
+    } else {
+        collide_pair<BF, false>(K, cp, lat, qs, qp, B, PairOvr{false, false, false}, x, y, z, c);
+    }
+}
+
 // streamed values of the uncovered ghost cells of a fine level
 template <bool BF>
 __global__ void k_ghost_stream16(const LowpK* __restrict__ K, const GhostCell* gl, long long n)
@@ -897,6 +1211,36 @@ __device__ __forceinline__ double widen_exact(float v)
     return __longlong_as_double((long long)bits);
 }
 
+// The sum of the eight children of one (coarse cell, direction, lattice) as
+// a fixed-point integer: with every exponent within 26 of the largest, the
+// FP64 sum of the eight values is exact (24-bit significands spread over at
+// most 26 + 24 bits, plus 3 bits of carry, fit FP64's 53), so the integer sum
+// rounded once to FP32 is exactly the FP64 sum rounded to FP32.  Returns
+// false (caller takes the FP64 adds) for a wider spread, a zero, a
+// subnormal, an infinity or a NaN.
+__device__ __forceinline__ bool sum8_exact(const float (&v)[8], float& out)
+{
+    unsigned emax = 0u, emin = 0xFFu;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const unsigned e = (__float_as_uint(v[k]) >> 23) & 0xFFu;
+        emax = max(emax, e);
+        emin = min(emin, e);
+    }
+    if (emin == 0u || emax == 0xFFu || emax - emin > 26u || emax < 60u) return false;
+    long long acc = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const unsigned u = __float_as_uint(v[k]);
+        const long long m = (long long)((u & 0x7FFFFFu) | 0x800000u) << (36u - (emax - ((u >> 23) & 0xFFu)));
+        acc += (u >> 31) ? -m : m;
+    }
+    // value = acc * 2^(emax - 150 - 36); the power of two is a normal float
+    // (emax >= 60) and the product of the rounded sum by it is exact
+    out = __ll2float_rn(acc) * __uint_as_float((emax - 59u) << 23);
+    return true;
+}
+
 template <bool BF>
 __global__ void __launch_bounds__(128) k_coalesce16(const LowpK* __restrict__ KC, const LowpK* __restrict__ KF,
                                                     const CoalesceCell* __restrict__ cl, long long n,
@@ -912,18 +1256,33 @@ __global__ void __launch_bounds__(128) k_coalesce16(const LowpK* __restrict__ KC
     const DevBox& A = F.box[cc.fbox];
     const long long cell = O.voff + val_lin(O, cc.cx, cc.cy, cc.cz);
     // the eight children's codes of both lattices, child k = 4 kz + 2 ky + kx;
-    // fixed offsets when all eight are valid cells of box A (the common case)
+    // fixed offsets when all eight are valid cells of box A (the common case),
+    // each x pair one aligned word (fine boxes sit on even cells, the padded
+    // layout puts valid cell 0 of a box on an even index)
     u16 code[2][8];
     if (cc.fx >= 0 && cc.fy >= 0 && cc.fz >= 0 && cc.fx + 1 < A.n[0] && cc.fy + 1 < A.n[1] && cc.fz + 1 < A.n[2]) {
         const long long b = (long long)q * F.N + A.voff + val_lin(A, cc.fx, cc.fy, cc.fz);
         const int sy = A.sy, sz = A.sz;
         const u16* __restrict__ f = KF->s.f + b;
         const u16* __restrict__ g = KF->s.g + b;
+        if ((b & 1) == 0) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int off = (k >> 2) * sz + ((k >> 1) & 1) * sy + (k & 1);
-            code[0][k] = __ldg(f + off);
-            code[1][k] = __ldg(g + off);
+            for (int r = 0; r < 4; ++r) {
+                const int off = (r >> 1) * sz + (r & 1) * sy;
+                const unsigned wf = __ldg(reinterpret_cast<const unsigned*>(f + off));
+                const unsigned wg = __ldg(reinterpret_cast<const unsigned*>(g + off));
+                code[0][2 * r] = (u16)(wf & 0xFFFFu);
+                code[0][2 * r + 1] = (u16)(wf >> 16);
+                code[1][2 * r] = (u16)(wg & 0xFFFFu);
+                code[1][2 * r + 1] = (u16)(wg >> 16);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const int off = (k >> 2) * sz + ((k >> 1) & 1) * sy + (k & 1);
+                code[0][k] = __ldg(f + off);
+                code[1][k] = __ldg(g + off);
+            }
         }
     } else {
 #pragma unroll
@@ -934,25 +1293,36 @@ __global__ void __launch_bounds__(128) k_coalesce16(const LowpK* __restrict__ KC
         }
     }
     // the mask test |v - (-1)| > SMALL_NUM on the FP32 decoded value; the sum
-    // in FP64, children in the reference's loop order (z, y, x)
+    // exact (sum8_exact) or in FP64, children in the reference's loop order
+    // (z, y, x)
     const float small_num = (float)(2.220446049250313e-16 * 1e10);
 #pragma unroll
     for (int lat = 0; lat < 2; ++lat) {
         const bool isg = lat == 1;
-        double sum = 0.0;
-        int vol = 0;
+        float fv[8];
+        bool all = true;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            const float fv = dec<BF>(KF->ct, code[lat][k], q, isg);
-            if (fabsf(fv + 1.0f) > small_num) { sum += widen_exact(fv); ++vol; }
+            fv[k] = dec<BF>(KF->ct, code[lat][k], q, isg);
+            all = all && fabsf(fv[k] + 1.0f) > small_num;
         }
         // all eight children unmasked is the common case: sum / 8 is exact,
         // and a power-of-two scaling commutes with the rounding to FP32 (the
         // values are far from the FP32 range limits), so it is applied after
+        float s8;
         u16 r;
-        if (vol > 0) r = enc<BF>(KC->ct, vol == 8 ? __double2float_rn(sum) * 0.125f : (float)(sum / (double)vol), q, isg);
-        else if (into_state) r = (isg ? KC->s.g : KC->s.f)[q * C.N + cell];
-        else r = NOOVR16;   // the step takes the cell's own streamed value
+        if (all && sum8_exact(fv, s8)) {
+            r = enc<BF>(KC->ct, s8 * 0.125f, q, isg);
+        } else {
+            double sum = 0.0;
+            int vol = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (fabsf(fv[k] + 1.0f) > small_num) { sum += widen_exact(fv[k]); ++vol; }
+            if (vol > 0) r = enc<BF>(KC->ct, vol == 8 ? __double2float_rn(sum) * 0.125f : (float)(sum / (double)vol), q, isg);
+            else if (into_state) r = (isg ? KC->s.g : KC->s.f)[q * C.N + cell];
+            else r = NOOVR16;   // the step takes the cell's own streamed value
+        }
         (isg ? go : fo)[q * C.N + cell] = r;
     }
 }
@@ -1128,17 +1498,43 @@ int Lowp16<BF>::fused_blocks_per_sm()
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_fused<BF>, FT_THREADS, 0) != cudaSuccess) nb = 1;
     return nb > 0 ? nb : 1;
 }
+// Q_corr pad face cells held by another box: a copy of that box's value
 template <bool BF>
-void Lowp16<BF>::two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
-                          int ntiles, const HaloCell* h, long long nh, float* qs, const QPtrs& qp, int tight,
-                          cudaStream_t s)
+__global__ void k_qpad_copy(const long long* __restrict__ dst, const long long* __restrict__ src, long long n,
+                            float* __restrict__ qs)
 {
-    if (ntiles == 0) return;
-    k_qcorr16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, tiles, qs, qp);
-    if (nh > 0) k_qhalo16<BF><<<(unsigned)((nh + 127) / 128), 128, 0, s>>>(k, h, nh, qs);
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) qs[dst[e]] = qs[src[e]];
+}
+
+template <bool BF>
+int Lowp16<BF>::two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
+                         int ntiles, const Tile* ptiles, int nptiles, const Tile* potiles, int nootiles,
+                         const QPad& qpad, float* qs, const QPtrs& qp, int tight, cudaStream_t s)
+{
+    int n = 0;
+    const CodecPair cp = nptiles + nootiles > 0 ? make_codec_pair(ct) : CodecPair{};
+    if (nptiles > 0) { k_qcorr16p<BF, false><<<nptiles, TILE_CELLS, 0, s>>>(k, cp, ptiles, qs, qp); ++n; }
+    if (nootiles > 0) { k_qcorr16p<BF, true><<<nootiles, TILE_CELLS, 0, s>>>(k, cp, potiles, qs, qp); ++n; }
+    if (ntiles > 0) { k_qcorr16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, tiles, qs, qp); ++n; }
+    if (n == 0) return 0;
+    if (qpad.ncopy > 0) {
+        k_qpad_copy<BF><<<(unsigned)((qpad.ncopy + 255) / 256), 256, 0, s>>>(qpad.dst, qpad.src, qpad.ncopy, qs);
+        ++n;
+    }
+    if (qpad.nghost > 0) {
+        k_qhalo16<BF><<<(unsigned)((qpad.nghost + 127) / 128), 128, 0, s>>>(k, qpad.ghost, qpad.nghost, qs);
+        ++n;
+    }
+    if (nptiles > 0) { k_collide16p<BF, false><<<nptiles, TILE_CELLS, 0, s>>>(k, cp, lat, ptiles, qs, qp); ++n; }
+    if (nootiles > 0) { k_collide16p<BF, true><<<nootiles, TILE_CELLS, 0, s>>>(k, cp, lat, potiles, qs, qp); ++n; }
     // register cap: 5 resident blocks per SM, or 6 with tight
-    if (tight) k_collide16<BF, 6><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs, qp);
-    else k_collide16<BF, 5><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs, qp);
+    if (ntiles > 0) {
+        if (tight) k_collide16<BF, 6><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs, qp);
+        else k_collide16<BF, 5><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs, qp);
+        ++n;
+    }
+    return n;
 }
 template <bool BF>
 void Lowp16<BF>::ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s)

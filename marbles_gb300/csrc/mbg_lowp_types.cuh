@@ -62,6 +62,18 @@ struct ExplodePlan {
     long long nx;
 };
 
+// Q_corr of the pad face cells that gradients read (inside the domain box,
+// fluid): copies from the valid cell of the owning box (qs indices d N + i),
+// and the pad cells on the coarse-fine shell, whose Q_corr is the moments of
+// the box's ghost fab (k_qhalo16)
+struct QPad {
+    const long long* dst = nullptr;
+    const long long* src = nullptr;
+    long long ncopy = 0;
+    const HaloCell* ghost = nullptr;
+    long long nghost = 0;
+};
+
 struct FusedTile {
     int box;
     short x0, y0, z0, z1;
@@ -71,14 +83,23 @@ struct FusedTile {
 
 // host helpers of the layout (mbg_lowp.cu), shared with the batched domains
 // (mbg_batch.cu)
-// step variants: 0 two-pass, 1 and 2 fused with runs of FUSED_ZC[v - 1]
-// planes, 3 two-pass with the collision pass capped at 80 registers
+// step variants: 0 two-pass (cell pairs where the box allows), 1 and 2
+// fused with runs of FUSED_ZC[v - 1] planes, 3 two-pass one cell per thread
+// with the collision pass capped at 80 registers
 constexpr int FUSED_ZC[2] = {4, 8};
 CodecTab make_codec(const mbg_params& p);
 Phys32 phys32(const mbg_params& p, double dt, const double idx[3]);
 long long pad_boxes(std::vector<DevBox>& box);
 std::vector<HaloCell> halo_cells(const std::vector<DevBox>& box);
 std::vector<FusedTile> fused_tiles(const std::vector<DevBox>& box, int zc);
+// the step's tile lists: pair tiles (PAIR_CELLS cells, two per thread) of
+// boxes with an even x extent whose cells one layer out are all fluid --
+// those without and those with a cell overwritten by coalescence (FL_OVR in
+// flags, the grown flag fabs of the boxes) -- and per-cell tiles
+// (TILE_CELLS) of the other boxes
+constexpr int PAIR_CELLS = 2 * TILE_CELLS;
+void step_tiles(const std::vector<DevBox>& box, const std::vector<uint8_t>* flags, std::vector<Tile>& pair,
+                std::vector<Tile>& pair_ovr, std::vector<Tile>& cell);
 
 // per-direction base pointers of the source and destination arrays of one
 // step (kernel parameters, so each population access is one 32-bit offset
@@ -111,10 +132,13 @@ struct Lowp16 {
     static void fused(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const FusedTile* t, int ntiles,
                       int grid, cudaStream_t s);
     static int fused_blocks_per_sm();   // resident CTAs of the fused step per SM
-    // the two-pass step: Q_corr pass, pad of Q_corr, collision pass (3 launches)
-    static void two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
-                         int ntiles, const HaloCell* h, long long nh, float* qs, const QPtrs& qp, int tight,
-                         cudaStream_t s);
+    // the two-pass step: Q_corr pass, pad of Q_corr, collision pass, over the
+    // pair tiles (two cells per thread, 256 cells per tile; potiles: those
+    // holding cells overwritten by coalescence) and the per-cell tiles;
+    // returns the launches made
+    static int two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
+                        int ntiles, const Tile* ptiles, int nptiles, const Tile* potiles, int nootiles,
+                        const QPad& qpad, float* qs, const QPtrs& qp, int tight, cudaStream_t s);
     static void ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s);
     // the ghost stream through its plan: gather, then the general entries
     static void ghost_gather(const LowpK* k, const long long* dst, const long long* src, long long n,

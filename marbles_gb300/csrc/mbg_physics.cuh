@@ -187,8 +187,8 @@ struct Equilibrium {
         return rf[ex + 1][ey + 1] * phz[ez + 1];
     }
 
-    template <int q>
-    __device__ __forceinline__ R geq(const Lattice<R>& lat) const
+    template <int q, class LT>
+    __device__ __forceinline__ R geq(const LT& lat) const
     {
         constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
         R f = grho;
@@ -207,9 +207,9 @@ struct Equilibrium {
 };
 
 // Source/LBM.cpp:646-760 for one fluid cell; returns omega (LBM.cpp:787-790)
-template <class R>
+template <class R, class LT>
 __device__ __forceinline__ R build_equilibrium(const Macro<R>& m, R dqx, R dqy, R dqz, R nu, R alpha, R dt,
-                                               R Rg, R cv, const Lattice<R>& lat, Equilibrium<R>& E)
+                                               R Rg, R cv, const LT& lat, Equilibrium<R>& E)
 {
     const R rho = m.rho;
     const R vel0 = m.u, vel1 = m.v, vel2 = m.w;

@@ -149,3 +149,64 @@ def test_autotune_keeps_state(prec):
     c64.step(18)
     c16.step(18)
     _check(_errors(c64, c16, levels), prec, TOL_PULSE_U[prec], TOL_PULSE_KE[prec])
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_pair_and_per_cell_steps_agree(prec):
+    """Variant 0 (two cells per thread, paired FP32) and variant 3 (one cell
+    per thread) on the two-level pulse, whose coarse level holds cells
+    overwritten by coalescence: both within the form's tolerance of FP64, and
+    within a few storage quanta of each other (their FP32 roundings differ:
+    the per-cell kernel contracts a * b + c, the paired one rounds twice)."""
+    import marbles_gb300 as M
+    p, levels = cases.gaussian_pulse(nc=32, fine_lo=8, fine_hi=23, mgs=16, width=3.0, t0=0.1)
+    c64, c16 = _pair(p, levels, prec)
+    o = cases.run_oracle(p, levels, 0)
+    c3 = M.Context(cases.mbg_params_from(p, prec))
+    for lev, b in enumerate(levels):
+        c3.define_level(lev, b, o.get_grown_flags(lev))
+        c3.set_state(lev, *o.get_state(lev))
+    c16.set_variant(0)
+    c3.set_variant(3)
+    for lev in range(len(levels)):
+        assert c16.tuning(lev)[0] == 0 and c3.tuning(lev)[0] == 3
+    c64.step(10)
+    c16.step(10)
+    c3.step(10)
+    _check(_errors(c64, c16, levels), prec, TOL_PULSE_U[prec], TOL_PULSE_KE[prec])
+    _check(_errors(c64, c3, levels), prec, TOL_PULSE_U[prec], TOL_PULSE_KE[prec])
+    q = 2.0 ** -11 if prec == 1 else 2.0 ** -8
+    for lev in range(len(levels)):
+        rho_a = c16.get_macro(lev).reshape(-1)
+        rho_b = c3.get_macro(lev).reshape(-1)
+        off = 0
+        worst = 0.0
+        for b in levels[lev]:
+            vol = int(np.prod(b[3:] - b[:3] + 1))
+            ra = rho_a[off:off + vol]
+            rb = rho_b[off:off + vol]
+            off += 19 * vol
+            worst = max(worst, float(np.max(np.abs(ra - rb) / rb)))
+        print("pair vs per-cell, level", lev, "rho", worst)
+        assert worst < 32 * q * 1e-2, (lev, worst)
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_nan_state_never_encodes_to_a_sentinel(prec):
+    """A NaN population makes the cell that pulls it NaN in every direction,
+    and in the next step the 27 cells around that one; the step's encoder
+    gives NaN codes there, never the -1 sentinel or the no-override code (the
+    paired kernels encode without a sentinel test)."""
+    import marbles_gb300 as M
+    p, levels = cases.taylor_green(16, 16, nu=0.1733333333333333)
+    o = cases.run_oracle(p, levels, 0)
+    c16 = M.Context(cases.mbg_params_from(p, prec))
+    c16.define_level(0, levels[0], o.get_grown_flags(0))
+    f, g = o.get_state(0)
+    f = f.copy()
+    f[5 * (f.size // 27) + 8 * 16 * 16 + 8 * 16 + 8] = np.nan   # direction 5 of cell (8, 8, 8)
+    c16.set_state(0, f, g)
+    c16.step(2)
+    f2, g2 = c16.get_state(0)
+    assert np.isnan(f2).sum() >= 27 * 27 and np.isnan(g2).sum() >= 27 * 27
+    assert not (f2 == -1.0).any() and not (g2 == -1.0).any()
