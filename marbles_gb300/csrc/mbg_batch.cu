@@ -107,9 +107,13 @@ static void launch_step(mbg_batch* b, int cur)
         // no pad of Q_corr: every domain face is one-sided
         const QPtrs qp = make_qptrs(b->f[cur], b->g[cur], b->f[1 - cur], b->g[1 - cur], b->N);
         const bool pairs = b->variant == 0;
+        PairLists pl;
+        if (pairs) {
+            pl.pair = b->ptiles;
+            pl.npair = b->nptiles;
+        }
         b->launches += 1 + LOWP16(b->bf, two_pass, k, b->ct, b->lat, pairs ? b->ctiles : b->tiles,
-                                  pairs ? b->nctiles : b->ntiles, b->ptiles, pairs ? b->nptiles : 0, nullptr, 0,
-                                  QPad{},
+                                  pairs ? b->nctiles : b->ntiles, pl, QPad{},
                                   b->qs, qp, !pairs, b->s);
     } else {
         const int v = b->variant - 1;
@@ -193,8 +197,9 @@ mbg_status mbg_batch_create(const mbg_params* common, int ndom, const mbg_domain
         for (long long s0 = 0; s0 < vol; s0 += TILE_CELLS) tiles.push_back(Tile{i, (int)s0});
     }
     b->ntiles = (int)tiles.size();
-    std::vector<Tile> ptiles, potiles, ctiles;
-    step_tiles(b->hbox, nullptr, ptiles, potiles, ctiles);
+    const StepTiles st_tiles = step_tiles(b->hbox, nullptr);   // every domain is fluid: pairs or per-cell
+    const std::vector<Tile>& ptiles = st_tiles.pair;
+    const std::vector<Tile>& ctiles = st_tiles.cell;
     b->nptiles = (int)ptiles.size();
     b->nctiles = (int)ctiles.size();
     mbg_status st = MBG_OK;

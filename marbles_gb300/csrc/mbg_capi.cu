@@ -54,6 +54,12 @@ struct Level {
     int ntiles = 0;
     NbrSlot* d_slots = nullptr;
     int* d_slot_off = nullptr;
+    NbrSlot* d_gslots = nullptr;       // FP64 ghost-shell tables (chunks 3 cells wide at the box faces)
+    int* d_gslot_off = nullptr;
+    GhostCell* d_ghost_fast = nullptr; // ghost cells of all-fluid boxes with a ghost-shell table
+    long long nghost_fast = 0;
+    GhostCell* d_ghost_gen = nullptr;  // the other ghost cells (general pull)
+    long long nghost_gen = 0;
     int slot_lg[3] = {0, 0, 0};
     int slot_max = 0;
     Tile* d_fast_tiles = nullptr;
@@ -117,6 +123,8 @@ struct mbg_ctx {
     double* d_red = nullptr;   // small reduction scratch
     double* d_out19 = nullptr;
     size_t out19_n = 0;
+    double* d_stage = nullptr;   // FP64 state transfers: one lattice of a level in host layout
+    size_t stage_n = 0;
     // per-block partial sums of the EB force (3 per tile of every level)
     double* d_partial = nullptr;
     size_t partial_n = 0;
@@ -245,14 +253,16 @@ static int owner_host(const Level& L, const int p[3])
     return L.omap[((size_t)bk * L.nb[1] + bj) * L.nb[0] + bi];
 }
 
-// Neighbour-slot tables of every box (NbrSlot): a chunk maps to one box when
+// Neighbour-slot tables of every box (NbrSlot), the chunks below and above
+// the box w cells wide (1 for the step's pulls, 3 for the pulls of the
+// coarse-fine ghost shell): a chunk maps to one box when
 // all its cells (after the periodic wrap) lie in that box's valid cells at
 // one fixed offset, or to the box's ghost fab when none lies in a box and the
 // box has one.  ok[n] is set when every chunk of box n maps (no non-periodic
 // domain side within one cell, no chunk across a box edge) and its table
 // fits; off[n] is the table's first slot, -1 for a box without one.
 static void build_slots(const Level& L, const int* is_periodic, const int lg[3], std::vector<NbrSlot>& out,
-                        std::vector<int>& off, std::vector<char>& ok)
+                        std::vector<int>& off, std::vector<char>& ok, int w = 1)
 {
     const int nbox = (int)L.boxes.size();
     out.clear();
@@ -279,8 +289,13 @@ static void build_slots(const Level& L, const int* is_periodic, const int lg[3],
                     int rlo[3], rhi[3];
                     bool inside = true;
                     for (int d = 0; d < 3; ++d) {
-                        if (c3[d] == 0) rlo[d] = rhi[d] = -1;
-                        else if (c3[d] == tc[d] - 1) rlo[d] = rhi[d] = b.n(d);
+                        if (c3[d] == 0) {
+                            rlo[d] = -w;
+                            rhi[d] = -1;
+                        } else if (c3[d] == tc[d] - 1) {
+                            rlo[d] = b.n(d);
+                            rhi[d] = b.n(d) + w - 1;
+                        }
                         else {
                             rlo[d] = (c3[d] - 1) << lg[d];
                             rhi[d] = std::min(c3[d] << lg[d], b.n(d)) - 1;
@@ -371,6 +386,12 @@ static void refresh_plan(mbg_ctx* ctx, Level& L)
     L.plan.ntiles = L.ntiles;
     L.plan.slots = L.d_slots;
     L.plan.slot_off = L.d_slot_off;
+    L.plan.gslots = L.d_gslots;
+    L.plan.gslot_off = L.d_gslot_off;
+    L.plan.ghost_fast = L.d_ghost_fast;
+    L.plan.nghost_fast = L.nghost_fast;
+    L.plan.ghost_gen = L.d_ghost_gen;
+    L.plan.nghost_gen = L.nghost_gen;
     for (int d = 0; d < 3; ++d) L.plan.slot_lg[d] = L.slot_lg[d];
     L.plan.slot_max = L.slot_max;
     L.plan.fast_tiles = L.d_fast_tiles;
@@ -790,6 +811,39 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
         MBG_CUDA(cudaMemcpyAsync(L.d_ghost, ghosts.data(), ghosts.size() * sizeof(GhostCell), cudaMemcpyHostToDevice, ctx->s));
     if (!ghosts1.empty())
         MBG_CUDA(cudaMemcpyAsync(L.d_ghost1, ghosts1.data(), ghosts1.size() * sizeof(GhostCell), cudaMemcpyHostToDevice, ctx->s));
+    // FP64 ghost stream: cells of all-fluid boxes whose ghost-shell chunks
+    // each map to one box or the ghost fab take the table pull
+    std::vector<NbrSlot> gslots;
+    std::vector<int> gslot_off;
+    std::vector<char> gslot_ok;
+    std::vector<GhostCell> gfast, ggen;
+    if (lev > 0 && p.precision == MBG_FP64 && !ghosts.empty()) {
+        build_slots(L, p.is_periodic, L.slot_lg, gslots, gslot_off, gslot_ok, 3);
+        for (const GhostCell& gc : ghosts) (gslot_ok[gc.box] && L.hbox[gc.box].all_fluid ? gfast : ggen).push_back(gc);
+        if ((st = dalloc(ctx, &L.d_gslots, gslots.size())) != MBG_OK) return st;
+        if ((st = dalloc(ctx, &L.d_gslot_off, gslot_off.size())) != MBG_OK) return st;
+        if ((st = dalloc(ctx, &L.d_ghost_fast, gfast.size())) != MBG_OK) return st;
+        if ((st = dalloc(ctx, &L.d_ghost_gen, ggen.size())) != MBG_OK) return st;
+        if (!gslots.empty())
+            MBG_CUDA(cudaMemcpyAsync(L.d_gslots, gslots.data(), gslots.size() * sizeof(NbrSlot), cudaMemcpyHostToDevice,
+                                     ctx->s));
+        MBG_CUDA(cudaMemcpyAsync(L.d_gslot_off, gslot_off.data(), gslot_off.size() * sizeof(int),
+                                 cudaMemcpyHostToDevice, ctx->s));
+        if (!gfast.empty())
+            MBG_CUDA(cudaMemcpyAsync(L.d_ghost_fast, gfast.data(), gfast.size() * sizeof(GhostCell),
+                                     cudaMemcpyHostToDevice, ctx->s));
+        if (!ggen.empty())
+            MBG_CUDA(cudaMemcpyAsync(L.d_ghost_gen, ggen.data(), ggen.size() * sizeof(GhostCell), cudaMemcpyHostToDevice,
+                                     ctx->s));
+    } else {
+        ggen = ghosts;
+        if ((st = dalloc(ctx, &L.d_ghost_gen, ggen.size())) != MBG_OK) return st;
+        if (!ggen.empty())
+            MBG_CUDA(cudaMemcpyAsync(L.d_ghost_gen, ggen.data(), ggen.size() * sizeof(GhostCell), cudaMemcpyHostToDevice,
+                                     ctx->s));
+    }
+    L.nghost_fast = (long long)gfast.size();
+    L.nghost_gen = (long long)ggen.size();
     if (p.precision == MBG_FP64) {
         for (int b = 0; b < 2; ++b) {
             if ((st = dalloc(ctx, &L.f[b], (size_t)L.N * NQ)) != MBG_OK) return st;
@@ -855,6 +909,28 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     return MBG_OK;
 }
 
+// the FP64 staging buffer, grown to one lattice of level L in host layout
+// (allocated at the first transfer of a level that size, not in the step)
+static mbg_status stage_buffer(mbg_ctx* ctx, const Level& L)
+{
+    const size_t need = (size_t)L.N * NQ;
+    if (ctx->stage_n >= need) return MBG_OK;
+    if (ctx->d_stage) {   // a smaller buffer of an earlier level: freed, not kept
+        MBG_CUDA(cudaStreamSynchronize(ctx->s));
+        for (auto& a : ctx->allocs)
+            if (a == ctx->d_stage) {
+                cudaFree(a);
+                a = nullptr;
+            }
+        ctx->d_stage = nullptr;
+        ctx->stage_n = 0;
+    }
+    mbg_status st = dalloc(ctx, &ctx->d_stage, need);
+    if (st != MBG_OK) return st;
+    ctx->stage_n = need;
+    return MBG_OK;
+}
+
 mbg_status mbg_set_state(mbg_ctx* ctx, int lev, const double* f, const double* g)
 {
     if (!ctx) return MBG_EINVAL;
@@ -866,18 +942,17 @@ mbg_status mbg_set_state(mbg_ctx* ctx, int lev, const double* f, const double* g
         ctx->launches += 2;
         return s2;
     }
-    long long off = 0;
-    for (size_t n = 0; n < L.boxes.size(); ++n) {
-        const long long vol = L.boxes[n].vol();
-        const long long voff = L.hbox[n].voff;
-        if (f)
-            MBG_CUDA(cudaMemcpy2DAsync(L.f[L.cur] + voff, L.N * sizeof(double), f + off * NQ, vol * sizeof(double),
-                                       vol * sizeof(double), NQ, cudaMemcpyHostToDevice, ctx->s));
-        if (g)
-            MBG_CUDA(cudaMemcpy2DAsync(L.g[L.cur] + voff, L.N * sizeof(double), g + off * NQ, vol * sizeof(double),
-                                       vol * sizeof(double), NQ, cudaMemcpyHostToDevice, ctx->s));
-        off += vol;
+    mbg_status st = stage_buffer(ctx, L);
+    if (st != MBG_OK) return st;
+    const size_t bytes = (size_t)L.N * NQ * sizeof(double);
+    for (int lat = 0; lat < 2; ++lat) {
+        const double* src = lat ? g : f;
+        if (!src) continue;
+        MBG_CUDA(cudaMemcpyAsync(ctx->d_stage, src, bytes, cudaMemcpyHostToDevice, ctx->s));
+        launch_stage(L.plan, ctx->d_stage, lat ? L.g[L.cur] : L.f[L.cur], 1, ctx->s);
+        ctx->launches++;
     }
+    MBG_CUDA(cudaGetLastError());
     MBG_CUDA(cudaStreamSynchronize(ctx->s));
     return MBG_OK;
 }
@@ -892,18 +967,17 @@ mbg_status mbg_get_state(mbg_ctx* ctx, int lev, double* f, double* g)
         ctx->launches += 2;
         return s2;
     }
-    long long off = 0;
-    for (size_t n = 0; n < L.boxes.size(); ++n) {
-        const long long vol = L.boxes[n].vol();
-        const long long voff = L.hbox[n].voff;
-        if (f)
-            MBG_CUDA(cudaMemcpy2DAsync(f + off * NQ, vol * sizeof(double), L.f[L.cur] + voff, L.N * sizeof(double),
-                                       vol * sizeof(double), NQ, cudaMemcpyDeviceToHost, ctx->s));
-        if (g)
-            MBG_CUDA(cudaMemcpy2DAsync(g + off * NQ, vol * sizeof(double), L.g[L.cur] + voff, L.N * sizeof(double),
-                                       vol * sizeof(double), NQ, cudaMemcpyDeviceToHost, ctx->s));
-        off += vol;
+    mbg_status st = stage_buffer(ctx, L);
+    if (st != MBG_OK) return st;
+    const size_t bytes = (size_t)L.N * NQ * sizeof(double);
+    for (int lat = 0; lat < 2; ++lat) {
+        double* dst = lat ? g : f;
+        if (!dst) continue;
+        launch_stage(L.plan, ctx->d_stage, lat ? L.g[L.cur] : L.f[L.cur], 0, ctx->s);
+        ctx->launches++;
+        MBG_CUDA(cudaMemcpyAsync(dst, ctx->d_stage, bytes, cudaMemcpyDeviceToHost, ctx->s));
     }
+    MBG_CUDA(cudaGetLastError());
     MBG_CUDA(cudaStreamSynchronize(ctx->s));
     return MBG_OK;
 }
@@ -986,7 +1060,7 @@ static mbg_status advance(mbg_ctx* ctx, int lev)
         timed(ctx, TK_GHOST_MOMENTS, [&] {
             launch_ghost_moments(L.plan, ph, L.fg[Bf], L.gg[Bf], L.gqc, ctx->s);
         });
-        ctx->launches += 2;
+        ctx->launches += ghost_stream_launches(L.plan) + (L.plan.nghost1 > 0);
     }
     timed(ctx, TK_MOMENTS, [&] {
         launch_moments(L.plan, ctx->bc, ph, L.f[A], L.g[A], L.fg[A], L.gg[A], L.f[Bf], L.g[Bf], L.md, ctx->s);

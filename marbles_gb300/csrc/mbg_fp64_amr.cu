@@ -72,8 +72,11 @@ __global__ void k_xslope(LV C, const int* __restrict__ ix, long long nx, const d
             const double back = 2.0 * (u0 - um);
             const double slp = (forw * back >= 0.0) ? fmin(fabs(forw), fabs(back)) : 0.0;
             o[(long long)(1 + d) * NQ * nx] = cen;
-            if (cen != 0.0) {
-                const double r = fmin(slp, fabs(cen)) / fabs(cen);
+            // r = min(slp, |cen|) / |cen| is exactly 1 unless slp < |cen|
+            // (x / x = 1), and only r < 1 lowers the limiter: the division
+            // runs only there
+            if (cen != 0.0 && slp < fabs(cen)) {
+                const double r = slp / fabs(cen);
                 if (r < 1.0)
                     atomicMin((unsigned long long*)&al[(lat * 3 + d) * nx + e],
                               (unsigned long long)__double_as_longlong(r));
@@ -175,7 +178,9 @@ __global__ void k_coalesce(LV C, LV F, BCParams P, Phys64 ph, MaskBits mb, const
                     }
         }
         double r;
-        if (cnt > 0) r = s / (double)cnt;
+        // s / 8 and s * 0.125 are the same correctly rounded value
+        if (cnt == 8) r = s * 0.125;
+        else if (cnt > 0) r = s / (double)cnt;
         else if (into_state) r = cA[q * C.N + cell];
         else r = __longlong_as_double(NOOVR64);   // the step pulls the cell's own streamed value
         (lat ? gcB : fcB)[q * C.N + cell] = r;

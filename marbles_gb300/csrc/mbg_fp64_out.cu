@@ -236,6 +236,33 @@ __global__ void __launch_bounds__(TILE_CELLS) k_conserved(LV L, Phys64 ph, const
         for (int k = 0; k < 5; ++k) atomicAdd(&out5[k], red[k][0]);
 }
 
+// host layout [box][q][cell] <-> the FP64 state [q][N]: the staging pass of
+// mbg_set_state / mbg_get_state (one contiguous copy over the link instead
+// of one strided copy per box and lattice)
+__global__ void __launch_bounds__(TILE_CELLS) k_stage(LV L, const Tile* tiles, double* stage, double* v,
+                                                      int to_state)
+{
+    int b, x, y, z;
+    long long c;
+    if (!cell_of_tile(L, tiles, b, x, y, z, c)) return;
+    const DevBox& B = L.box[b];
+    const long long vol = (long long)B.n[0] * B.n[1] * B.n[2];
+    double* h = stage + B.hoff * NQ + c;
+    double* d = v + B.voff + c;
+    if (to_state) {
+#pragma unroll 9
+        for (int q = 0; q < NQ; ++q) d[q * L.N] = h[q * vol];
+    } else {
+#pragma unroll 9
+        for (int q = 0; q < NQ; ++q) h[q * vol] = d[q * L.N];
+    }
+}
+
+void launch_stage(const LevelPlan& lp, double* stage, double* v, int to_state, cudaStream_t s)
+{
+    if (lp.ntiles > 0) k_stage<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, lp.tiles, stage, v, to_state);
+}
+
 void launch_macro_local(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, double* out19,
                         cudaStream_t s)
 {

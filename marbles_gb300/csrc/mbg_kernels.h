@@ -98,6 +98,15 @@ struct LevelPlan {
     int ngen = 0;
     const GhostCell* ghost_list = nullptr;   // all uncovered ghost cells
     long long nghost_cells = 0;
+    // FP64 ghost stream: ghost-shell slot tables (chunks 3 cells wide at the
+    // box faces, the step tables' grain inside), the ghost cells that pull
+    // through them and the others
+    const NbrSlot* gslots = nullptr;
+    const int* gslot_off = nullptr;
+    const GhostCell* ghost_fast = nullptr;
+    long long nghost_fast = 0;
+    const GhostCell* ghost_gen = nullptr;
+    long long nghost_gen = 0;
     const GhostCell* ghost_list1 = nullptr;  // first ghost layer only
     long long nghost1 = 0;
     // FP64 explosion: each ghost cell's slot, the slots' coarse cells, and per
@@ -136,6 +145,8 @@ void launch_interp_level(const LevelPlan& fine, const LevelPlan& crse, const dou
                          cudaStream_t s);
 // kernel launches of one launch_moments or launch_collide call
 int fp64_step_launches(const LevelPlan& lp);
+// kernel launches of one launch_ghost_stream call
+int ghost_stream_launches(const LevelPlan& lp);
 void launch_ghost_stream(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA,
                          const double* gA, const double* fAg, const double* gAg, double* fBg, double* gBg,
                          cudaStream_t s);
@@ -149,6 +160,8 @@ void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParam
                      const CoalesceCell* list, long long n, const double* ff, const double* gf, const double* ffg,
                      const double* gfg, const double* fcA, const double* gcA, const double* fcAg,
                      const double* gcAg, double* fcB, double* gcB, int into_state, cudaStream_t s);
+// host layout [box][q][cell] (stage) <-> FP64 state v [q][N], to_state: into v
+void launch_stage(const LevelPlan& lp, double* stage, double* v, int to_state, cudaStream_t s);
 void launch_macro_local(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, double* out19,
                         cudaStream_t s);
 // per-block partial force sums (3 per tile) of one level; launch_sum_partials

@@ -32,16 +32,20 @@ struct LowpDev {
     double variant_ms[4] = {0, 0, 0, 0};   // tuner's timings (0: not timed)
     float* qs = nullptr;         // Q_corr of the two-pass step, [3][N]
     QPad qpad;                   // Q_corr of the pad (qpad_plan)
-    Tile* ptiles = nullptr;      // variant 0: pair tiles without / with overwritten cells, per-cell
-    int nptiles = 0;             // tiles (step_tiles); the pair lists hold room for every pair tile
+    // variant 0: the tile classes of step_tiles; each device list holds room
+    // for every tile of its kind, so that lowp_retile only copies
+    Tile* ptiles = nullptr;
+    int nptiles = 0;
     Tile* potiles = nullptr;
     int nootiles = 0;
+    Tile* petiles = nullptr;
+    int neetiles = 0;
     Tile* ctiles = nullptr;
     int nctiles = 0;
+    unsigned* nmask = nullptr;   // neighbour masks (neighbour_masks), or null
     std::vector<DevBox> box16h;  // host copy of box16
     HaloCell* halo = nullptr;    // every pad cell of every box
-    long long* gdst = nullptr;   // pad fill by gather: destination and source indices
-    long long* gsrc = nullptr;
+    HaloCopy* hcopy = nullptr;   // pad fill: per pad cell, the directions and the cell copied (halo_plan)
     long long ngather = 0;
     HaloCell* general = nullptr; // pad cells that need the general kernel (physical BCs)
     long long ngeneral = 0;
@@ -163,44 +167,85 @@ long long pad_boxes(std::vector<DevBox>& box)
     return np + (np & 1);
 }
 
-void step_tiles(const std::vector<DevBox>& box, const std::vector<uint8_t>* flags, std::vector<Tile>& pair,
-                std::vector<Tile>& pair_ovr, std::vector<Tile>& cell)
+static void upload_tiles(LowpDev* D, const StepTiles& t, cudaStream_t s)
 {
-    pair.clear();
-    pair_ovr.clear();
-    cell.clear();
+    D->nptiles = (int)t.pair.size();
+    D->nootiles = (int)t.pair_ovr.size();
+    D->neetiles = (int)t.pair_eb.size();
+    D->nctiles = (int)t.cell.size();
+    if (!t.pair.empty()) cudaMemcpyAsync(D->ptiles, t.pair.data(), t.pair.size() * sizeof(Tile), cudaMemcpyHostToDevice, s);
+    if (!t.pair_ovr.empty())
+        cudaMemcpyAsync(D->potiles, t.pair_ovr.data(), t.pair_ovr.size() * sizeof(Tile), cudaMemcpyHostToDevice, s);
+    if (!t.pair_eb.empty())
+        cudaMemcpyAsync(D->petiles, t.pair_eb.data(), t.pair_eb.size() * sizeof(Tile), cudaMemcpyHostToDevice, s);
+    if (!t.cell.empty()) cudaMemcpyAsync(D->ctiles, t.cell.data(), t.cell.size() * sizeof(Tile), cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);   // the host vectors end with the caller
+}
+
+StepTiles step_tiles(const std::vector<DevBox>& box, const std::vector<uint8_t>* flags)
+{
+    StepTiles t;
     for (size_t n = 0; n < box.size(); ++n) {
         const DevBox& B = box[n];
         const long long vol = (long long)B.n[0] * B.n[1] * B.n[2];
-        if (B.n[0] % 2 == 0 && B.vfluid && B.voff % 2 == 0) {
-            for (long long s = 0; s < vol; s += PAIR_CELLS) {
-                bool ovr = false;
-                for (long long c = s; c < std::min(vol, s + PAIR_CELLS) && flags && !ovr; ++c) {
-                    const int x = (int)(c % B.n[0]), y = (int)((c / B.n[0]) % B.n[1]), z = (int)(c / B.n[0] / B.n[1]);
-                    const long long fi = B.foff + ((long long)(z + 3) * (B.n[1] + 6) + (y + 3)) * (B.n[0] + 6) + (x + 3);
-                    ovr = (*flags)[fi] & FL_OVR;
-                }
-                (ovr ? pair_ovr : pair).push_back(Tile{(int)n, (int)s});
+        const bool pairs = B.n[0] % 2 == 0 && B.voff % 2 == 0;
+        if (!pairs) {
+            for (long long s = 0; s < vol; s += TILE_CELLS) t.cell.push_back(Tile{(int)n, (int)s});
+            continue;
+        }
+        for (long long s = 0; s < vol; s += PAIR_CELLS) {
+            bool ovr = false;
+            for (long long c = s; c < std::min(vol, s + PAIR_CELLS) && flags && !ovr; ++c) {
+                const int x = (int)(c % B.n[0]), y = (int)((c / B.n[0]) % B.n[1]), z = (int)(c / B.n[0] / B.n[1]);
+                const long long fi = B.foff + ((long long)(z + 3) * (B.n[1] + 6) + (y + 3)) * (B.n[0] + 6) + (x + 3);
+                ovr = (*flags)[fi] & FL_OVR;
             }
-        } else {
-            for (long long s = 0; s < vol; s += TILE_CELLS) cell.push_back(Tile{(int)n, (int)s});
+            if (B.vfluid) {
+                (ovr ? t.pair_ovr : t.pair).push_back(Tile{(int)n, (int)s});
+            } else if (!ovr) {
+                t.pair_eb.push_back(Tile{(int)n, (int)s});
+            } else {
+                // overwritten cells next to solids: the per-cell kernels
+                for (long long c = s; c < std::min(vol, s + PAIR_CELLS); c += TILE_CELLS)
+                    t.cell.push_back(Tile{(int)n, (int)c});
+            }
         }
     }
+    return t;
 }
 
-// the pair tile lists again after the level's flags gained or lost cells
-// overwritten by coalescence (a finer level defined or dropped)
+// per valid cell of the boxes holding solid cells: bit q where the fluid
+// cell's source x - e_q is solid, bit NMASK_FLUID where the cell is fluid
+static std::vector<unsigned> neighbour_masks(const std::vector<DevBox>& box, const std::vector<uint8_t>& fl,
+                                             long long N)
+{
+    std::vector<unsigned> m((size_t)N, 0u);
+    for (const DevBox& B : box) {
+        if (B.vfluid) continue;
+        auto f = [&](int x, int y, int z) {
+            return fl[B.foff + ((long long)(z + 3) * (B.n[1] + 6) + (y + 3)) * (B.n[0] + 6) + (x + 3)] & FL_FLUID;
+        };
+        for (int z = 0; z < B.n[2]; ++z)
+            for (int y = 0; y < B.n[1]; ++y)
+                for (int x = 0; x < B.n[0]; ++x) {
+                    if (!f(x, y, z)) continue;
+                    unsigned w = 1u << NMASK_FLUID;
+                    for (int q = 0; q < NQ; ++q)
+                        if (!f(x - ev_x(q), y - ev_y(q), z - ev_z(q))) w |= 1u << q;
+                    m[B.voff + (long long)z * B.sz + (long long)y * B.sy + x] = w;
+                }
+    }
+    return m;
+}
+
+// the step's tile lists again after the level's flags gained or lost cells
+// overwritten by coalescence (a finer level defined or dropped); the device
+// lists were sized at set-up for every class
 void lowp_retile(LowpLevel& L, const std::vector<uint8_t>& flags, cudaStream_t s)
 {
     LowpDev* D = dev_of(L);
     if (!D) return;
-    std::vector<Tile> pt, po, ctl;
-    step_tiles(D->box16h, &flags, pt, po, ctl);
-    D->nptiles = (int)pt.size();
-    D->nootiles = (int)po.size();
-    if (!pt.empty()) cudaMemcpyAsync(D->ptiles, pt.data(), pt.size() * sizeof(Tile), cudaMemcpyHostToDevice, s);
-    if (!po.empty()) cudaMemcpyAsync(D->potiles, po.data(), po.size() * sizeof(Tile), cudaMemcpyHostToDevice, s);
-    cudaStreamSynchronize(s);   // the host vectors end here
+    upload_tiles(D, step_tiles(D->box16h, &flags), s);
 }
 
 // every pad cell of every box, faces first, then edges, then corners, so that
@@ -281,15 +326,15 @@ static void qpad_plan(const std::vector<DevBox>& box, const std::vector<HaloCell
     }
 }
 
-// Pad fill plan: for every (pad cell, inward direction) whose target is a
-// fluid cell and whose source is a fluid cell inside the domain, the storage
-// index the value is copied from -- a valid cell of the owning box (periodic
-// images resolved) as q N + index, or the box's own ghost fab as
-// -(q NG + index) - 1.  Pad cells with a source outside a non-periodic side
+// Pad fill plan: per pad cell, the directions q whose pull from the pad cell
+// lands on a fluid cell of the box (the pad cell fluid too: a solid source
+// bounces back in the step), and the storage index within one component the
+// values are copied from -- a valid cell of the owning box (periodic images
+// resolved), or the box's own ghost fab as -index - 1.  Every direction of a
+// pad cell copies from the same cell.  Pad cells outside a non-periodic side
 // (physical BC) go to a separate list filled by the general kernel.
-static void halo_plan(const std::vector<DevBox>& box, const std::vector<HaloCell>& halo, long long N, long long NG,
-                      const LevelHost& h, std::vector<long long>& dst, std::vector<long long>& src,
-                      std::vector<HaloCell>& general)
+static void halo_plan(const std::vector<DevBox>& box, const std::vector<HaloCell>& halo, const LevelHost& h,
+                      std::vector<HaloCopy>& copies, std::vector<HaloCell>& general)
 {
     auto fab = [](const DevBox& B, int x, int y, int z) {
         return ((long long)(z + 3) * (B.n[1] + 6) + (y + 3)) * (B.n[0] + 6) + (x + 3);
@@ -297,40 +342,44 @@ static void halo_plan(const std::vector<DevBox>& box, const std::vector<HaloCell
     const std::vector<uint8_t>& fl = *h.flags;
     for (const HaloCell& c : halo) {
         const DevBox& B = box[c.box];
-        const uint8_t sf = fl[B.foff + fab(B, c.x, c.y, c.z)];
-        bool gen = false;
-        for (int q = 0; q < NQ && !gen; ++q) {
+        if (!(fl[B.foff + fab(B, c.x, c.y, c.z)] & FL_FLUID)) continue;   // bounce-back in the step
+        unsigned qmask = 0u;
+        for (int q = 0; q < NQ; ++q) {
             const int tx = c.x + ev_x(q), ty = c.y + ev_y(q), tz = c.z + ev_z(q);
             if (tx < 0 || ty < 0 || tz < 0 || tx >= B.n[0] || ty >= B.n[1] || tz >= B.n[2]) continue;
-            if (!(fl[B.foff + fab(B, tx, ty, tz)] & FL_FLUID)) continue;   // target not collided
-            if (!(sf & FL_FLUID)) continue;                                   // bounce-back in the step
-            int gp[3] = {B.lo[0] + c.x, B.lo[1] + c.y, B.lo[2] + c.z};
-            bool out = false;
-            for (int d = 0; d < 3; ++d) {
-                if (gp[d] < h.dlo[d] || gp[d] > h.dhi[d]) {
-                    if (!h.per[d]) { out = true; break; }
-                    const int len = h.dhi[d] - h.dlo[d] + 1;
-                    gp[d] = h.dlo[d] + (((gp[d] - h.dlo[d]) % len) + len) % len;
-                }
-            }
-            if (out) { gen = true; break; }
-            const int bi = (gp[0] - h.dlo[0]) / h.G[0], bj = (gp[1] - h.dlo[1]) / h.G[1], bk = (gp[2] - h.dlo[2]) / h.G[2];
-            const int o = (*h.omap)[((size_t)bk * h.nb[1] + bj) * h.nb[0] + bi];
-            long long sidx;
-            if (o >= 0) {
-                const DevBox& O = box[o];
-                sidx = (long long)q * N + O.voff + (long long)(gp[2] - O.lo[2]) * O.sz +
-                       (long long)(gp[1] - O.lo[1]) * O.sy + (gp[0] - O.lo[0]);
-            } else if (B.goff >= 0) {
-                sidx = -((long long)q * NG + B.goff + fab(B, c.x, c.y, c.z)) - 1;
-            } else {
-                gen = true;
-                break;
-            }
-            dst.push_back((long long)q * N + B.voff + (long long)c.z * B.sz + (long long)c.y * B.sy + c.x);
-            src.push_back(sidx);
+            if (fl[B.foff + fab(B, tx, ty, tz)] & FL_FLUID) qmask |= 1u << q;   // a collided target
         }
-        if (gen) general.push_back(c);
+        if (!qmask) continue;
+        int gp[3] = {B.lo[0] + c.x, B.lo[1] + c.y, B.lo[2] + c.z};
+        bool out = false;
+        for (int d = 0; d < 3; ++d) {
+            if (gp[d] < h.dlo[d] || gp[d] > h.dhi[d]) {
+                if (!h.per[d]) { out = true; break; }
+                const int len = h.dhi[d] - h.dlo[d] + 1;
+                gp[d] = h.dlo[d] + (((gp[d] - h.dlo[d]) % len) + len) % len;
+            }
+        }
+        if (out) {
+            general.push_back(c);
+            continue;
+        }
+        const int bi = (gp[0] - h.dlo[0]) / h.G[0], bj = (gp[1] - h.dlo[1]) / h.G[1], bk = (gp[2] - h.dlo[2]) / h.G[2];
+        const int o = (*h.omap)[((size_t)bk * h.nb[1] + bj) * h.nb[0] + bi];
+        HaloCopy hc;
+        hc.dst = B.voff + (long long)c.z * B.sz + (long long)c.y * B.sy + c.x;
+        hc.qmask = qmask;
+        hc.pad = 0;
+        if (o >= 0) {
+            const DevBox& O = box[o];
+            hc.src = O.voff + (long long)(gp[2] - O.lo[2]) * O.sz + (long long)(gp[1] - O.lo[1]) * O.sy +
+                     (gp[0] - O.lo[0]);
+        } else if (B.goff >= 0) {
+            hc.src = -(B.goff + fab(B, c.x, c.y, c.z)) - 1;
+        } else {
+            general.push_back(c);
+            continue;
+        }
+        copies.push_back(hc);
     }
 }
 
@@ -467,10 +516,9 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
         return MBG_EINVAL;
     }
     const std::vector<HaloCell> halo = halo_cells(box);
-    std::vector<long long> gdst, gsrc;
+    std::vector<HaloCopy> hcopy;
     std::vector<HaloCell> general;
-    halo_plan(box, halo, L.N, NG, host, gdst, gsrc, general);
-    sort_plan(gdst, gsrc);
+    halo_plan(box, halo, host, hcopy, general);
     std::vector<long long> sdst, ssrc;
     std::vector<int> scell, sq;
     if (host.ghosts && NG > 0) ghost_plan(box, *host.ghosts, L.N, NG, host, sdst, ssrc, scell, sq);
@@ -488,19 +536,23 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
         cudaMemcpy(D->ftiles[v], tiles.data(), tiles.size() * sizeof(FusedTile), cudaMemcpyHostToDevice);
     }
     {
-        std::vector<Tile> pt, po, ctl;
-        step_tiles(box, host.flags, pt, po, ctl);
-        D->nptiles = (int)pt.size();
-        D->nootiles = (int)po.size();
-        D->nctiles = (int)ctl.size();
-        const size_t cap = pt.size() + po.size();
+        const StepTiles t = step_tiles(box, host.flags);
+        const size_t cap = t.pair.size() + t.pair_ovr.size() + t.pair_eb.size();   // pair tiles of any class
+        size_t ccap = 0;                                                         // every cell per-cell
+        for (const DevBox& B : box) ccap += ((size_t)B.n[0] * B.n[1] * B.n[2] + TILE_CELLS - 1) / TILE_CELLS;
         if ((st = lalloc(L, (void**)&D->ptiles, cap * sizeof(Tile), err)) != MBG_OK) return st;
         if ((st = lalloc(L, (void**)&D->potiles, cap * sizeof(Tile), err)) != MBG_OK) return st;
-        if ((st = lalloc(L, (void**)&D->ctiles, ctl.size() * sizeof(Tile), err)) != MBG_OK) return st;
-        cudaMemcpy(D->ptiles, pt.data(), pt.size() * sizeof(Tile), cudaMemcpyHostToDevice);
-        cudaMemcpy(D->potiles, po.data(), po.size() * sizeof(Tile), cudaMemcpyHostToDevice);
-        cudaMemcpy(D->ctiles, ctl.data(), ctl.size() * sizeof(Tile), cudaMemcpyHostToDevice);
+        if ((st = lalloc(L, (void**)&D->petiles, cap * sizeof(Tile), err)) != MBG_OK) return st;
+        if ((st = lalloc(L, (void**)&D->ctiles, ccap * sizeof(Tile), err)) != MBG_OK) return st;
+        upload_tiles(D, t, 0);
         D->box16h = box;
+        bool any_eb = false;
+        for (const DevBox& B : box) any_eb = any_eb || !B.vfluid;
+        if (any_eb) {
+            const std::vector<unsigned> m = neighbour_masks(box, *host.flags, L.N);
+            if ((st = lalloc(L, (void**)&D->nmask, m.size() * sizeof(unsigned), err)) != MBG_OK) return st;
+            cudaMemcpy(D->nmask, m.data(), m.size() * sizeof(unsigned), cudaMemcpyHostToDevice);
+        }
     }
     {
         long long* qd = nullptr;
@@ -519,13 +571,11 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
         D->qpad.nghost = (long long)qghost.size();
     }
     if ((st = lalloc(L, (void**)&D->halo, halo.size() * sizeof(HaloCell), err)) != MBG_OK) return st;
-    D->ngather = (long long)gdst.size();
+    D->ngather = (long long)hcopy.size();
     D->ngeneral = (long long)general.size();
-    if ((st = lalloc(L, (void**)&D->gdst, gdst.size() * sizeof(long long), err)) != MBG_OK) return st;
-    if ((st = lalloc(L, (void**)&D->gsrc, gsrc.size() * sizeof(long long), err)) != MBG_OK) return st;
+    if ((st = lalloc(L, (void**)&D->hcopy, hcopy.size() * sizeof(HaloCopy), err)) != MBG_OK) return st;
     if ((st = lalloc(L, (void**)&D->general, general.size() * sizeof(HaloCell), err)) != MBG_OK) return st;
-    cudaMemcpy(D->gdst, gdst.data(), gdst.size() * sizeof(long long), cudaMemcpyHostToDevice);
-    cudaMemcpy(D->gsrc, gsrc.data(), gsrc.size() * sizeof(long long), cudaMemcpyHostToDevice);
+    cudaMemcpy(D->hcopy, hcopy.data(), hcopy.size() * sizeof(HaloCopy), cudaMemcpyHostToDevice);
     cudaMemcpy(D->general, general.data(), general.size() * sizeof(HaloCell), cudaMemcpyHostToDevice);
     D->nsgather = (long long)sdst.size();
     D->nsgen = (long long)scell.size();
@@ -609,6 +659,7 @@ static void upload_k(LowpLevel& L, const LevelPlan& plan, const BCParams& bc, bo
         k.fBg = (u16*)L.fg[1 - a];
         k.gBg = (u16*)L.gg[1 - a];
         k.phys = nullptr;
+        k.nmask = D->nmask;
     }
     cudaMemcpyAsync(D->dk, D->hk, 2 * sizeof(LowpK), cudaMemcpyHostToDevice, s);
     cudaStreamSynchronize(s);
@@ -737,7 +788,7 @@ int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const Le
     }
     if (D->nhalo > 0) {
         run(LOWP_STAGE_HALO, [&] {
-            LOWP16(bf, halo_gather, k, D->gdst, D->gsrc, D->ngather, s);
+            LOWP16(bf, halo_copy, k, D->hcopy, D->ngather, s);
             LOWP16(bf, halo, k, D->general, D->ngeneral, s);
         });
         ++launches;
@@ -755,8 +806,16 @@ int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const Le
         run(LOWP_STAGE_FUSED,
             [&] {
                 const QPtrs qp = make_qptrs(L.f[A], L.g[A], L.f[1 - A], L.g[1 - A], L.N);
-                launches += LOWP16(bf, two_pass, k, D->ct, D->lat, ct, nct, D->ptiles, pairs ? D->nptiles : 0,
-                                   D->potiles, pairs ? D->nootiles : 0, D->qpad, D->qs, qp, !pairs, s);
+                PairLists pl;
+                if (pairs) {
+                    pl.pair = D->ptiles;
+                    pl.npair = D->nptiles;
+                    pl.pair_ovr = D->potiles;
+                    pl.npair_ovr = D->nootiles;
+                    pl.pair_eb = D->petiles;
+                    pl.npair_eb = D->neetiles;
+                }
+                launches += LOWP16(bf, two_pass, k, D->ct, D->lat, ct, nct, pl, D->qpad, D->qs, qp, !pairs, s);
             });
     } else {
         const int v = D->variant - 1;

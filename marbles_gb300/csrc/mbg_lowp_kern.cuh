@@ -173,21 +173,27 @@ __global__ void k_halo16(const LowpK* __restrict__ K, const HaloCell* __restrict
 #undef MBG_HF16
 }
 
-// pad fill by gather (the plan of mbg_lowp.cu::halo_plan): a copy of f and
-// g from a valid cell (src >= 0) or the box's ghost fab (src < 0)
+// pad fill along the plan of mbg_lowp.cu::halo_plan: one thread per pad
+// cell, a copy of f and g for each direction of its mask from one valid cell
+// (src >= 0) or the box's ghost fab (src < 0); the cells of one face share
+// their mask, so warps run the same directions
 template <bool BF>
-__global__ void k_halo_gather16(const LowpK* __restrict__ K, const long long* __restrict__ dst,
-                                const long long* __restrict__ src, long long n)
+__global__ void k_halo_copy16(const LowpK* __restrict__ K, const HaloCopy* __restrict__ hc, long long n)
 {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
-    const long long d = dst[e], s_ = src[e];
-    if (s_ >= 0) {
-        K->fA[d] = K->s.f[s_];
-        K->gA[d] = K->s.g[s_];
-    } else {
-        K->fA[d] = K->s.fg[-s_ - 1];
-        K->gA[d] = K->s.gg[-s_ - 1];
+    const HaloCopy h = hc[e];
+    const long long N = K->L.N, NG = K->L.NG;
+    const bool own = h.src >= 0;
+    const u16* __restrict__ f = own ? K->s.f + h.src : K->s.fg + (-h.src - 1);
+    const u16* __restrict__ g = own ? K->s.g + h.src : K->s.gg + (-h.src - 1);
+    const long long stride = own ? N : NG;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        if ((h.qmask >> q) & 1u) {
+            K->fA[q * N + h.dst] = f[q * stride];
+            K->gA[q * N + h.dst] = g[q * stride];
+        }
     }
 }
 
@@ -857,10 +863,29 @@ __device__ __forceinline__ F2 dec_pair(unsigned w, float2 sc, float2 rest)
     return fma2(F2(h2f_pair<BF>(w)), F2(sc), F2(rest));
 }
 
+// boxes holding solid cells: a fluid cell whose source x - e_q is solid
+// (bit q of its neighbour mask m0 / m1) takes its own opposite population,
+// decoded with the opposite direction's codec (the half-way bounce-back of
+// the push, Source/LBM.cpp:574-598); v: the pulled pair already decoded
+template <bool BF, int q, bool PIN>
+__device__ __forceinline__ F2 bounce(F2 v, const u16* __restrict__ vopp, int c, unsigned m0, unsigned m1,
+                                     float2 sc_opp, float2 rest_opp)
+{
+    const unsigned b0 = (m0 >> q) & 1u, b1 = (m1 >> q) & 1u;
+    if (b0 | b1) {
+        const unsigned own = PIN ? ld_pin32(vopp + c) : __ldg(reinterpret_cast<const unsigned*>(vopp + c));
+        const F2 vb = fma2(F2(h2f_pair<BF>(own)), F2(sc_opp), F2(rest_opp));
+        if (b0) v.v.x = vb.v.x;
+        if (b1) v.v.y = vb.v.y;
+    }
+    return v;
+}
+
 // moments of a pair: MERGE for pass 1, else the pass-2 selection
-template <bool BF, bool MERGE, bool OVR = false>
+template <bool BF, bool MERGE, bool OVR = false, bool EB = false>
 __device__ __forceinline__ MomentAcc<F2> moments_pair(const LowpK* __restrict__ K, const CodecPair& cp,
-                                                      const QPtrs& qp, const PairOvr& o, int c, int sy, int sz)
+                                                      const QPtrs& qp, const PairOvr& o, int c, int sy, int sz,
+                                                      unsigned m0 = 0u, unsigned m1 = 0u)
 {
     u16* __restrict__ fo = const_cast<u16*>(K->s.fo);
     u16* __restrict__ go = const_cast<u16*>(K->s.go);
@@ -880,8 +905,14 @@ __device__ __forceinline__ MomentAcc<F2> moments_pair(const LowpK* __restrict__ 
     MomentAcc<F2> acc;
     static_for<0, NQ>([&](auto Q) {
         constexpr int q = Q.value;
-        acc.template add<q>(dec_pair<BF, q>(wf[q], cp.fsc[q], cp.frest[q]),
-                            dec_pair<BF, q>(wg[q], cp.gsc[q], cp.grest[q]));
+        F2 vf = dec_pair<BF, q>(wf[q], cp.fsc[q], cp.frest[q]);
+        F2 vg = dec_pair<BF, q>(wg[q], cp.gsc[q], cp.grest[q]);
+        if constexpr (EB) {
+            constexpr int oq = opp(q);
+            vf = bounce<BF, q, false>(vf, qp.f[oq], c, m0, m1, cp.fsc[oq], cp.frest[oq]);
+            vg = bounce<BF, q, false>(vg, qp.g[oq], c, m0, m1, cp.gsc[oq], cp.grest[oq]);
+        }
+        acc.template add<q>(vf, vg);
     });
     return acc;
 }
@@ -890,34 +921,56 @@ __device__ __forceinline__ MomentAcc<F2> moments_pair(const LowpK* __restrict__ 
 // per component)
 // OVR: a tile holding cells overwritten by coalescence (the others never
 // look at flags or override buffers)
-template <bool BF, bool OVR>
+// EB: a tile of a box holding solid cells (never with OVR): bounce-back by
+// the neighbour masks, Q_corr 0 at solid cells
+template <bool BF, bool OVR, bool EB>
 __global__ void __launch_bounds__(TILE_CELLS) k_qcorr16p(const LowpK* __restrict__ K, const CodecPair cp,
                                                          const Tile* __restrict__ tiles, float* __restrict__ qs,
                                                          const QPtrs qp)
 {
+    static_assert(!(OVR && EB), "tiles with overwritten cells next to solids run per cell");
     const LV16& L = K->L;
     const Tile t = tiles[blockIdx.x];
     const DevBox& B = L.box[t.box];
     int x, y, z;
     if (!pair_cell(B, t, x, y, z)) return;
     const int c = (int)(B.voff + val_lin(B, x, y, z));
-    const PairOvr o = OVR ? pair_ovr<BF>(K, B, x, y, z) : PairOvr{false, false, false};
-    const Macro<F2> m =
-        moments_pair<BF, true>(K, cp, qp, o, c, B.sy, B.sz).finish(F2(K->ph.mesh_speed), F2(K->ph.Rg), F2(K->ph.cv));
     const long long N = L.N;
-    *reinterpret_cast<float2*>(qs + c) = m.qcx.v;
-    *reinterpret_cast<float2*>(qs + N + c) = m.qcy.v;
-    *reinterpret_cast<float2*>(qs + 2 * N + c) = m.qcz.v;
+    unsigned m0 = 0u, m1 = 0u;
+    if constexpr (EB) {
+        const uint2 mm = *reinterpret_cast<const uint2*>(K->nmask + c);
+        m0 = mm.x;
+        m1 = mm.y;
+        if (!(((m0 | m1) >> NMASK_FLUID) & 1u)) {
+            const float2 zero = make_float2(0.f, 0.f);
+            *reinterpret_cast<float2*>(qs + c) = zero;
+            *reinterpret_cast<float2*>(qs + N + c) = zero;
+            *reinterpret_cast<float2*>(qs + 2 * N + c) = zero;
+            return;
+        }
+    }
+    const PairOvr o = OVR ? pair_ovr<BF>(K, B, x, y, z) : PairOvr{false, false, false};
+    const Macro<F2> m = moments_pair<BF, true, false, EB>(K, cp, qp, o, c, B.sy, B.sz, m0, m1)
+                            .finish(F2(K->ph.mesh_speed), F2(K->ph.Rg), F2(K->ph.cv));
+    float2 qx = m.qcx.v, qy = m.qcy.v, qz = m.qcz.v;
+    if constexpr (EB) {
+        if (!((m0 >> NMASK_FLUID) & 1u)) qx.x = qy.x = qz.x = 0.f;
+        if (!((m1 >> NMASK_FLUID) & 1u)) qx.y = qy.y = qz.y = 0.f;
+    }
+    *reinterpret_cast<float2*>(qs + c) = qx;
+    *reinterpret_cast<float2*>(qs + N + c) = qy;
+    *reinterpret_cast<float2*>(qs + 2 * N + c) = qz;
 }
 
 // relaxation and encoding of the three directions (ex, ey, -1 .. 1) of a
 // cell pair: f_eq = rf[ex][ey] phz[ez] (Equilibrium::feq); g_eq of
 // Equilibrium::geq regrouped as w_q (b + A4[ez^2] / 2 + ez cz) with b and cz
 // shared by the three, so that few partial sums are live at a time
-template <bool BF, int ex, int ey, bool OVR>
+template <bool BF, int ex, int ey, bool OVR, bool EB>
 __device__ __forceinline__ void relax_group(const LowpK* __restrict__ K, const CodecPair& cp,
                                             const Lattice<float>& lat, const QPtrs& qp, const PairOvr& o,
-                                            const Equilibrium<F2>& E, F2 omega, F2 h0, F2 h1, int c, int sy, int sz)
+                                            const Equilibrium<F2>& E, F2 omega, F2 h0, F2 h1, int c, int sy, int sz,
+                                            unsigned m0, unsigned m1, unsigned solid)
 {
     const F2 half(0.5f);
     F2 s2 = E.A1[ex * ex] + E.A2[ey * ey];
@@ -936,61 +989,86 @@ __device__ __forceinline__ void relax_group(const LowpK* __restrict__ K, const C
     static_for<0, 3>([&](auto Z) {
         constexpr int ez = Z.value - 1;
         constexpr int q = find_dir(ex, ey, ez);
-        const F2 fq = dec_pair<BF, q>(code_sel<q, true>(qp.f[q], fo, N, OVR, c, sy, sz), cp.fsc[q], cp.frest[q]);
+        const unsigned wf = code_sel<q, true>(qp.f[q], fo, N, OVR, c, sy, sz);
+        const unsigned wg = code_sel<q, true>(qp.g[q], go, N, OVR, c, sy, sz);
+        constexpr int oq = opp(q);
+        F2 fq = dec_pair<BF, q>(wf, cp.fsc[q], cp.frest[q]);
+        if constexpr (EB) fq = bounce<BF, q, true>(fq, qp.f[oq], c, m0, m1, cp.fsc[oq], cp.frest[oq]);
         const F2 fn = fma2(omega, E.rf[ex + 1][ey + 1] * E.phz[ez + 1] - fq, fq);
-        *reinterpret_cast<unsigned*>(qp.fo[q] + c) = f2h_pair<BF>(((fn - F2(cp.frest[q])) * F2(cp.fisc[q])).v);
+        // solid cells keep the stream sentinel (all bits set)
+        *reinterpret_cast<unsigned*>(qp.fo[q] + c) =
+            f2h_pair<BF>(((fn - F2(cp.frest[q])) * F2(cp.fisc[q])).v) | solid;
         const F2 gsum = ez == 0 ? b + h0 : (ez == 1 ? b1 + cz : b1 - cz);
         const F2 geq = gsum * F2(lat.w[q]);
-        const F2 gq = dec_pair<BF, q>(code_sel<q, true>(qp.g[q], go, N, OVR, c, sy, sz), cp.gsc[q], cp.grest[q]);
+        F2 gq = dec_pair<BF, q>(wg, cp.gsc[q], cp.grest[q]);
+        if constexpr (EB) gq = bounce<BF, q, true>(gq, qp.g[oq], c, m0, m1, cp.gsc[oq], cp.grest[oq]);
         const F2 gn = fma2(omega, geq - gq, gq);
-        *reinterpret_cast<unsigned*>(qp.go[q] + c) = f2h_pair<BF>(((gn - F2(cp.grest[q])) * F2(cp.gisc[q])).v);
+        *reinterpret_cast<unsigned*>(qp.go[q] + c) =
+            f2h_pair<BF>(((gn - F2(cp.grest[q])) * F2(cp.gisc[q])).v) | solid;
     });
 }
 
 // pass 2 on pairs: moments again from the same codes, q-correction
 // gradient, equilibria, relaxation, encoding (OVR: a pair with a cell
-// overwritten by coalescence, its codes read from the override buffers)
-template <bool BF, bool OVR>
+// overwritten by coalescence, its codes read from the override buffers; EB:
+// a box holding solid cells, bounce-back and presence by the neighbour
+// masks m0 / m1, solid cells keep the sentinel)
+template <bool BF, bool OVR, bool EB>
 __device__ __forceinline__ void collide_pair(const LowpK* __restrict__ K, const CodecPair& cp,
                                              const Lattice<float>& lat, const float* __restrict__ qs, const QPtrs& qp,
-                                             const DevBox& B, const PairOvr& o, int x, int y, int z, int c)
+                                             const DevBox& B, const PairOvr& o, int x, int y, int z, int c,
+                                             unsigned m0, unsigned m1)
 {
     const LV16& L = K->L;
     const int sy = B.sy, sz = B.sz;
     const Phys32* __restrict__ PH = K->phys ? K->phys + B.phys : &K->ph;
     const float Rg = K->ph.Rg, cv = K->ph.cv;
-    const Macro<F2> m =
-        moments_pair<BF, false, OVR>(K, cp, qp, o, c, sy, sz).finish(F2(K->ph.mesh_speed), F2(Rg), F2(cv));
+    const Macro<F2> m = moments_pair<BF, false, OVR, EB>(K, cp, qp, o, c, sy, sz, m0, m1)
+                            .finish(F2(K->ph.mesh_speed), F2(Rg), F2(cv));
     // gradient() of Source/Utilities.H:279-312: the x neighbours inside the
-    // pair are the other cell's own value
+    // pair are the other cell's own value; in EB boxes a solid neighbour is
+    // not on the stencil (the source of direction -e along the axis)
     const long long N = L.N;
     const float xm = qs[c - 1], xp = qs[c + 2];
     const float2 ym = *reinterpret_cast<const float2*>(qs + N + c - sy);
     const float2 yp = *reinterpret_cast<const float2*>(qs + N + c + sy);
     const float2 zm = *reinterpret_cast<const float2*>(qs + 2 * N + c - sz);
     const float2 zp = *reinterpret_cast<const float2*>(qs + 2 * N + c + sz);
-    const bool px0 = present_vf(L, B, x, 0, 1), mx0 = present_vf(L, B, x, 0, -1);
-    const bool px1 = present_vf(L, B, x + 1, 0, 1), mx1 = present_vf(L, B, x + 1, 0, -1);
+    constexpr int QXP = find_dir(-1, 0, 0), QXM = find_dir(1, 0, 0);   // sources x + 1, x - 1
+    constexpr int QYP = find_dir(0, -1, 0), QYM = find_dir(0, 1, 0);
+    constexpr int QZP = find_dir(0, 0, -1), QZM = find_dir(0, 0, 1);
+    auto fl = [&](unsigned mk, int q) { return !EB || !((mk >> q) & 1u); };
+    const bool px0 = present_vf(L, B, x, 0, 1) && fl(m0, QXP), mx0 = present_vf(L, B, x, 0, -1) && fl(m0, QXM);
+    const bool px1 = present_vf(L, B, x + 1, 0, 1) && fl(m1, QXP), mx1 = present_vf(L, B, x + 1, 0, -1) && fl(m1, QXM);
     const bool py = present_vf(L, B, y, 1, 1), my = present_vf(L, B, y, 1, -1);
     const bool pz = present_vf(L, B, z, 2, 1), mz = present_vf(L, B, z, 2, -1);
     const float ix = PH->idx[0], iy = PH->idx[1], iz = PH->idx[2];
     const F2 dqx(grad1(px0, mx0, m.qcx.v.y, m.qcx.v.x, xm, ix), grad1(px1, mx1, xp, m.qcx.v.y, m.qcx.v.x, ix));
-    const F2 dqy(grad1(py, my, yp.x, m.qcy.v.x, ym.x, iy), grad1(py, my, yp.y, m.qcy.v.y, ym.y, iy));
-    const F2 dqz(grad1(pz, mz, zp.x, m.qcz.v.x, zm.x, iz), grad1(pz, mz, zp.y, m.qcz.v.y, zm.y, iz));
+    const F2 dqy(grad1(py && fl(m0, QYP), my && fl(m0, QYM), yp.x, m.qcy.v.x, ym.x, iy),
+                 grad1(py && fl(m1, QYP), my && fl(m1, QYM), yp.y, m.qcy.v.y, ym.y, iy));
+    const F2 dqz(grad1(pz && fl(m0, QZP), mz && fl(m0, QZM), zp.x, m.qcz.v.x, zm.x, iz),
+                 grad1(pz && fl(m1, QZP), mz && fl(m1, QZM), zp.y, m.qcz.v.y, zm.y, iz));
     Equilibrium<F2> E;
     const F2 omega = build_equilibrium<F2>(m, dqx, dqy, dqz, F2(PH->nu), F2(PH->alpha), F2(PH->dt), F2(Rg), F2(cv),
                                            lat, E);
     const F2 h0 = F2(0.5f) * E.A4[0], h1 = F2(0.5f) * E.A4[1];
+    unsigned solid = 0u;
+    if constexpr (EB) {
+        if (!((m0 >> NMASK_FLUID) & 1u)) solid |= 0x0000FFFFu;
+        if (!((m1 >> NMASK_FLUID) & 1u)) solid |= 0xFFFF0000u;
+    }
     static_for<0, 9>([&](auto G) {
-        relax_group<BF, G.value % 3 - 1, G.value / 3 - 1, OVR>(K, cp, lat, qp, o, E, omega, h0, h1, c, sy, sz);
+        relax_group<BF, G.value % 3 - 1, G.value / 3 - 1, OVR, EB>(K, cp, lat, qp, o, E, omega, h0, h1, c, sy, sz,
+                                                                   m0, m1, solid);
     });
 }
 
-template <bool BF, bool OVR>
-__global__ void __launch_bounds__(TILE_CELLS, 4) k_collide16p(const LowpK* __restrict__ K, const CodecPair cp,
+template <bool BF, bool OVR, bool EB>
+__global__ void __launch_bounds__(TILE_CELLS, EB ? 3 : 4) k_collide16p(const LowpK* __restrict__ K, const CodecPair cp,
                                                            const Lattice<float> lat, const Tile* __restrict__ tiles,
                                                            const float* __restrict__ qs, const QPtrs qp)
 {
+    static_assert(!(OVR && EB), "tiles with overwritten cells next to solids run per cell");
     const LV16& L = K->L;
     const Tile t = tiles[blockIdx.x];
     const DevBox& B = L.box[t.box];
@@ -999,10 +1077,22 @@ __global__ void __launch_bounds__(TILE_CELLS, 4) k_collide16p(const LowpK* __res
     const int c = (int)(B.voff + val_lin(B, x, y, z));
     if constexpr (OVR) {
         const PairOvr o = pair_ovr<BF>(K, B, x, y, z);
-        if (o.any) collide_pair<BF, true>(K, cp, lat, qs, qp, B, o, x, y, z, c);
-        else collide_pair<BF, false>(K, cp, lat, qs, qp, B, o, x, y, z, c);
+        if (o.any) collide_pair<BF, true, false>(K, cp, lat, qs, qp, B, o, x, y, z, c, 0u, 0u);
+        else collide_pair<BF, false, false>(K, cp, lat, qs, qp, B, o, x, y, z, c, 0u, 0u);
+    } else if constexpr (EB) {
+        const uint2 mm = *reinterpret_cast<const uint2*>(K->nmask + c);
+        if (!(((mm.x | mm.y) >> NMASK_FLUID) & 1u)) {
+            // two solid cells: the stream sentinel in every direction
+#pragma unroll
+            for (int q = 0; q < NQ; ++q) {
+                *reinterpret_cast<unsigned*>(qp.fo[q] + c) = 0xFFFFFFFFu;
+                *reinterpret_cast<unsigned*>(qp.go[q] + c) = 0xFFFFFFFFu;
+            }
+            return;
+        }
+        collide_pair<BF, false, true>(K, cp, lat, qs, qp, B, PairOvr{false, false, false}, x, y, z, c, mm.x, mm.y);
     } else {
-        collide_pair<BF, false>(K, cp, lat, qs, qp, B, PairOvr{false, false, false}, x, y, z, c);
+        collide_pair<BF, false, false>(K, cp, lat, qs, qp, B, PairOvr{false, false, false}, x, y, z, c, 0u, 0u);
     }
 }
 
@@ -1134,8 +1224,9 @@ __global__ void k_xslope16(const LowpK* __restrict__ KC, const int* __restrict__
             const float back = 2.0f * (u0 - um);
             const float slp = (forw * back >= 0.f) ? fminf(fabsf(forw), fabsf(back)) : 0.f;
             o[(long long)(1 + d) * NQ * nx] = cen;
-            if (cen != 0.f) {
-                const float r = fminf(slp, fabsf(cen)) / fabsf(cen);
+            // the ratio is exactly 1 unless slp < |cen|: divide only there
+            if (cen != 0.f && slp < fabsf(cen)) {
+                const float r = slp / fabsf(cen);
                 if (r < 1.0f) atomicMin((int*)&al[(lat * 3 + d) * nx + e], __float_as_int(r));
             }
         }
@@ -1476,9 +1567,9 @@ void Lowp16<BF>::halo(const LowpK* k, const HaloCell* h, long long n, cudaStream
     if (n > 0) k_halo16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, h, n);
 }
 template <bool BF>
-void Lowp16<BF>::halo_gather(const LowpK* k, const long long* dst, const long long* src, long long n, cudaStream_t s)
+void Lowp16<BF>::halo_copy(const LowpK* k, const HaloCopy* hc, long long n, cudaStream_t s)
 {
-    if (n > 0) k_halo_gather16<BF><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(k, dst, src, n);
+    if (n > 0) k_halo_copy16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, hc, n);
 }
 template <bool BF>
 void Lowp16<BF>::halo_periodic(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s)
@@ -1509,13 +1600,21 @@ __global__ void k_qpad_copy(const long long* __restrict__ dst, const long long* 
 
 template <bool BF>
 int Lowp16<BF>::two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
-                         int ntiles, const Tile* ptiles, int nptiles, const Tile* potiles, int nootiles,
-                         const QPad& qpad, float* qs, const QPtrs& qp, int tight, cudaStream_t s)
+                         int ntiles, const PairLists& pl, const QPad& qpad, float* qs, const QPtrs& qp, int tight,
+                         cudaStream_t s)
 {
     int n = 0;
-    const CodecPair cp = nptiles + nootiles > 0 ? make_codec_pair(ct) : CodecPair{};
-    if (nptiles > 0) { k_qcorr16p<BF, false><<<nptiles, TILE_CELLS, 0, s>>>(k, cp, ptiles, qs, qp); ++n; }
-    if (nootiles > 0) { k_qcorr16p<BF, true><<<nootiles, TILE_CELLS, 0, s>>>(k, cp, potiles, qs, qp); ++n; }
+    const bool any_pair = pl.npair + pl.npair_ovr + pl.npair_eb > 0;
+    const CodecPair cp = any_pair ? make_codec_pair(ct) : CodecPair{};
+    if (pl.npair > 0) { k_qcorr16p<BF, false, false><<<pl.npair, TILE_CELLS, 0, s>>>(k, cp, pl.pair, qs, qp); ++n; }
+    if (pl.npair_ovr > 0) {
+        k_qcorr16p<BF, true, false><<<pl.npair_ovr, TILE_CELLS, 0, s>>>(k, cp, pl.pair_ovr, qs, qp);
+        ++n;
+    }
+    if (pl.npair_eb > 0) {
+        k_qcorr16p<BF, false, true><<<pl.npair_eb, TILE_CELLS, 0, s>>>(k, cp, pl.pair_eb, qs, qp);
+        ++n;
+    }
     if (ntiles > 0) { k_qcorr16<BF><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, tiles, qs, qp); ++n; }
     if (n == 0) return 0;
     if (qpad.ncopy > 0) {
@@ -1526,8 +1625,18 @@ int Lowp16<BF>::two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float
         k_qhalo16<BF><<<(unsigned)((qpad.nghost + 127) / 128), 128, 0, s>>>(k, qpad.ghost, qpad.nghost, qs);
         ++n;
     }
-    if (nptiles > 0) { k_collide16p<BF, false><<<nptiles, TILE_CELLS, 0, s>>>(k, cp, lat, ptiles, qs, qp); ++n; }
-    if (nootiles > 0) { k_collide16p<BF, true><<<nootiles, TILE_CELLS, 0, s>>>(k, cp, lat, potiles, qs, qp); ++n; }
+    if (pl.npair > 0) {
+        k_collide16p<BF, false, false><<<pl.npair, TILE_CELLS, 0, s>>>(k, cp, lat, pl.pair, qs, qp);
+        ++n;
+    }
+    if (pl.npair_ovr > 0) {
+        k_collide16p<BF, true, false><<<pl.npair_ovr, TILE_CELLS, 0, s>>>(k, cp, lat, pl.pair_ovr, qs, qp);
+        ++n;
+    }
+    if (pl.npair_eb > 0) {
+        k_collide16p<BF, false, true><<<pl.npair_eb, TILE_CELLS, 0, s>>>(k, cp, lat, pl.pair_eb, qs, qp);
+        ++n;
+    }
     // register cap: 5 resident blocks per SM, or 6 with tight
     if (ntiles > 0) {
         if (tight) k_collide16<BF, 6><<<ntiles, TILE_CELLS, 0, s>>>(k, ct, lat, tiles, qs, qp);

@@ -39,12 +39,27 @@ struct LowpK {
     u16 *fA, *gA;                  // the source again, writable (its pad is filled in place)
     u16 *fB, *gB, *fBg, *gBg;      // destination: the other buffer
     const Phys32* phys;            // per-box parameters (batched domains), or null: ph for all boxes
+    // per valid cell of boxes holding solid cells, at the cell's storage
+    // index: bit q (0 .. 26) set where the fluid cell's source x - e_q is
+    // solid, bit NMASK_FLUID where the cell is fluid (null: no such boxes)
+    const unsigned* nmask;
 };
+constexpr int NMASK_FLUID = 27;
 
 // one cell of a box's pad: box-local coordinates, each -1 .. n
 struct HaloCell {
     int box;
     short x, y, z, pad;
+};
+
+// pad fill of one pad cell: for each direction q in qmask, component q of
+// storage index dst takes component q of src (a valid cell, or the ghost fab
+// index -src - 1)
+struct HaloCopy {
+    long long dst;
+    long long src;
+    unsigned qmask;
+    unsigned pad;
 };
 
 // explosion plan of a fine level: the distinct coarse cells under its
@@ -74,6 +89,16 @@ struct QPad {
     long long nghost = 0;
 };
 
+// the device pair tile lists of a step (StepTiles)
+struct PairLists {
+    const Tile* pair = nullptr;
+    int npair = 0;
+    const Tile* pair_ovr = nullptr;
+    int npair_ovr = 0;
+    const Tile* pair_eb = nullptr;
+    int npair_eb = 0;
+};
+
 struct FusedTile {
     int box;
     short x0, y0, z0, z1;
@@ -98,8 +123,13 @@ std::vector<FusedTile> fused_tiles(const std::vector<DevBox>& box, int zc);
 // flags, the grown flag fabs of the boxes) -- and per-cell tiles
 // (TILE_CELLS) of the other boxes
 constexpr int PAIR_CELLS = 2 * TILE_CELLS;
-void step_tiles(const std::vector<DevBox>& box, const std::vector<uint8_t>* flags, std::vector<Tile>& pair,
-                std::vector<Tile>& pair_ovr, std::vector<Tile>& cell);
+struct StepTiles {
+    std::vector<Tile> pair;       // pair tiles of boxes fluid one cell out
+    std::vector<Tile> pair_ovr;   // the same holding cells overwritten by coalescence
+    std::vector<Tile> pair_eb;    // pair tiles of boxes holding solid cells (no overwritten cell)
+    std::vector<Tile> cell;       // per-cell tiles of the rest
+};
+StepTiles step_tiles(const std::vector<DevBox>& box, const std::vector<uint8_t>* flags);
 
 // per-direction base pointers of the source and destination arrays of one
 // step (kernel parameters, so each population access is one 32-bit offset
@@ -127,18 +157,17 @@ inline QPtrs make_qptrs(const void* f, const void* g, void* fo, void* go, long l
 template <bool BF>
 struct Lowp16 {
     static void halo(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s);
-    static void halo_gather(const LowpK* k, const long long* dst, const long long* src, long long n, cudaStream_t s);
+    static void halo_copy(const LowpK* k, const HaloCopy* hc, long long n, cudaStream_t s);
     static void halo_periodic(const LowpK* k, const HaloCell* h, long long n, cudaStream_t s);
     static void fused(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const FusedTile* t, int ntiles,
                       int grid, cudaStream_t s);
     static int fused_blocks_per_sm();   // resident CTAs of the fused step per SM
     // the two-pass step: Q_corr pass, pad of Q_corr, collision pass, over the
-    // pair tiles (two cells per thread, 256 cells per tile; potiles: those
-    // holding cells overwritten by coalescence) and the per-cell tiles;
-    // returns the launches made
+    // pair tiles (two cells per thread, 256 cells per tile; see StepTiles)
+    // and the per-cell tiles; returns the launches made
     static int two_pass(const LowpK* k, const CodecTab& ct, const Lattice<float>& lat, const Tile* tiles,
-                        int ntiles, const Tile* ptiles, int nptiles, const Tile* potiles, int nootiles,
-                        const QPad& qpad, float* qs, const QPtrs& qp, int tight, cudaStream_t s);
+                        int ntiles, const PairLists& pl, const QPad& qpad, float* qs, const QPtrs& qp, int tight,
+                        cudaStream_t s);
     static void ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s);
     // the ghost stream through its plan: gather, then the general entries
     static void ghost_gather(const LowpK* k, const long long* dst, const long long* src, long long n,
