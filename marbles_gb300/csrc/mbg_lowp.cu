@@ -49,7 +49,14 @@ struct LowpDev {
     long long ngather = 0;
     HaloCell* general = nullptr; // pad cells that need the general kernel (physical BCs)
     long long ngeneral = 0;
-    long long* sdst = nullptr;   // ghost stream by gather (ghost_plan)
+    NbrSlot* gslots = nullptr;   // ghost stream: ghost-shell slot tables (ghost_slots16), the ghost
+    int* gslot_off = nullptr;    // cells that copy through them, the other ghost cells (gathered)
+    int gslot_lg[3] = {0, 0, 0};
+    GhostCell* ghost_fast = nullptr;
+    long long nghost_fast = 0;
+    GhostCell* ghost_rest = nullptr;
+    long long nghost_rest = 0;
+    long long* sdst = nullptr;   // ghost stream by gather (ghost_plan over the other ghost cells)
     long long* ssrc = nullptr;
     long long nsgather = 0;
     int* scell = nullptr;        // ghost stream entries for the general kernel
@@ -389,6 +396,104 @@ static void halo_plan(const std::vector<DevBox>& box, const std::vector<HaloCell
 // or the -1 sentinel (src = -1).  Bounce-back from a solid source (a value
 // of the opposite direction, re-encoded) and physical BCs go to the general
 // list as (ghost-cell index, direction).
+// Ghost-shell slot tables on the padded layout (chunks 3 cells wide at the
+// box faces, grain 2^lg inside): each chunk of the box grown by 3 maps to
+// one box's valid cells at a fixed offset or to the box's own ghost fab;
+// ok[n] when every chunk of box n does.  The ghost stream of an all-fluid
+// box with a table is then a copy through it (k_ghost_stream16s).
+static void ghost_slots16(const std::vector<DevBox>& box, const LevelHost& h, const int lg[3],
+                          std::vector<NbrSlot>& out, std::vector<int>& off, std::vector<char>& ok)
+{
+    const int w = 3;
+    const int nbox = (int)box.size();
+    out.clear();
+    off.assign(nbox, -1);
+    ok.assign(nbox, 0);
+    auto owner = [&](int p[3]) -> int {
+        for (int d = 0; d < 3; ++d) {
+            if (p[d] < h.dlo[d] || p[d] > h.dhi[d]) {
+                if (!h.per[d]) return -2;
+                const int len = h.dhi[d] - h.dlo[d] + 1;
+                p[d] = h.dlo[d] + (((p[d] - h.dlo[d]) % len) + len) % len;
+            }
+        }
+        const int bi = (p[0] - h.dlo[0]) / h.G[0], bj = (p[1] - h.dlo[1]) / h.G[1], bk = (p[2] - h.dlo[2]) / h.G[2];
+        return (*h.omap)[((size_t)bk * h.nb[1] + bj) * h.nb[0] + bi];
+    };
+    for (int n = 0; n < nbox; ++n) {
+        const DevBox& B = box[n];
+        if (!B.all_fluid || B.goff < 0) continue;
+        int tc[3];
+        for (int d = 0; d < 3; ++d) tc[d] = ((B.n[d] + (1 << lg[d]) - 1) >> lg[d]) + 2;
+        const long long T = (long long)tc[0] * tc[1] * tc[2];
+        if (T > SLOT_TABLE_MAX) continue;
+        const size_t t0 = out.size();
+        out.resize(t0 + (size_t)T, NbrSlot{0, 0, 0, -1, 0});
+        bool all = true;
+        for (int cz = 0; cz < tc[2] && all; ++cz)
+            for (int cy = 0; cy < tc[1] && all; ++cy)
+                for (int cx = 0; cx < tc[0] && all; ++cx) {
+                    const int c3[3] = {cx, cy, cz};
+                    NbrSlot& S = out[t0 + cx + (size_t)tc[0] * (cy + (size_t)tc[1] * cz)];
+                    int rlo[3], rhi[3];
+                    bool inside = true;
+                    for (int d = 0; d < 3; ++d) {
+                        if (c3[d] == 0) { rlo[d] = -w; rhi[d] = -1; }
+                        else if (c3[d] == tc[d] - 1) { rlo[d] = B.n[d]; rhi[d] = B.n[d] + w - 1; }
+                        else { rlo[d] = (c3[d] - 1) << lg[d]; rhi[d] = std::min(c3[d] << lg[d], B.n[d]) - 1; }
+                        inside = inside && c3[d] > 0 && c3[d] < tc[d] - 1;
+                    }
+                    if (inside) {
+                        S.base = B.voff;
+                        S.sy = B.sy;
+                        S.sz = B.sz;
+                        S.ghost = 0;
+                        continue;
+                    }
+                    int own = -3, dl0[3] = {0, 0, 0};
+                    for (int z = rlo[2]; z <= rhi[2] && all; ++z)
+                        for (int y = rlo[1]; y <= rhi[1] && all; ++y)
+                            for (int x = rlo[0]; x <= rhi[0] && all; ++x) {
+                                int p[3] = {B.lo[0] + x, B.lo[1] + y, B.lo[2] + z};
+                                const int o = owner(p);
+                                if (o == -2) { all = false; break; }
+                                int dl[3] = {0, 0, 0};
+                                if (o >= 0) {
+                                    dl[0] = p[0] - box[o].lo[0] - x;
+                                    dl[1] = p[1] - box[o].lo[1] - y;
+                                    dl[2] = p[2] - box[o].lo[2] - z;
+                                }
+                                if (own == -3) {
+                                    own = o;
+                                    for (int d = 0; d < 3; ++d) dl0[d] = dl[d];
+                                } else if (o != own || dl[0] != dl0[0] || dl[1] != dl0[1] || dl[2] != dl0[2]) {
+                                    all = false;
+                                }
+                            }
+                    if (!all) break;
+                    if (own >= 0) {
+                        const DevBox& O = box[own];
+                        S.base = O.voff + (long long)dl0[2] * O.sz + (long long)dl0[1] * O.sy + dl0[0];
+                        S.sy = O.sy;
+                        S.sz = O.sz;
+                        S.ghost = 0;
+                    } else {
+                        const int gx = B.n[0] + 6, gy = B.n[1] + 6;
+                        S.base = B.goff + 3LL * gy * gx + 3LL * gx + 3;
+                        S.sy = gx;
+                        S.sz = gx * gy;
+                        S.ghost = 1;
+                    }
+                }
+        if (!all) {
+            out.resize(t0);
+            continue;
+        }
+        off[n] = (int)t0;
+        ok[n] = 1;
+    }
+}
+
 static void ghost_plan(const std::vector<DevBox>& box, const std::vector<GhostCell>& gl, long long N, long long NG,
                        const LevelHost& h, std::vector<long long>& dst, std::vector<long long>& src,
                        std::vector<int>& gen_cell, std::vector<int>& gen_q)
@@ -521,7 +626,15 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     halo_plan(box, halo, host, hcopy, general);
     std::vector<long long> sdst, ssrc;
     std::vector<int> scell, sq;
-    if (host.ghosts && NG > 0) ghost_plan(box, *host.ghosts, L.N, NG, host, sdst, ssrc, scell, sq);
+    std::vector<NbrSlot> gsl;
+    std::vector<int> gsl_off;
+    std::vector<GhostCell> gfast, grest;
+    if (host.ghosts && NG > 0) {
+        std::vector<char> gok;
+        ghost_slots16(box, host, plan.slot_lg, gsl, gsl_off, gok);
+        for (const GhostCell& gc : *host.ghosts) (gok[gc.box] ? gfast : grest).push_back(gc);
+        ghost_plan(box, grest, L.N, NG, host, sdst, ssrc, scell, sq);
+    }
     sort_plan(sdst, ssrc);
     D->nhalo = (long long)halo.size();
     std::vector<long long> qdst, qsrc;
@@ -577,6 +690,17 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     if ((st = lalloc(L, (void**)&D->general, general.size() * sizeof(HaloCell), err)) != MBG_OK) return st;
     cudaMemcpy(D->hcopy, hcopy.data(), hcopy.size() * sizeof(HaloCopy), cudaMemcpyHostToDevice);
     cudaMemcpy(D->general, general.data(), general.size() * sizeof(HaloCell), cudaMemcpyHostToDevice);
+    D->nghost_fast = (long long)gfast.size();
+    D->nghost_rest = (long long)grest.size();
+    for (int d = 0; d < 3; ++d) D->gslot_lg[d] = plan.slot_lg[d];
+    if ((st = lalloc(L, (void**)&D->gslots, gsl.size() * sizeof(NbrSlot), err)) != MBG_OK) return st;
+    if ((st = lalloc(L, (void**)&D->gslot_off, gsl_off.size() * sizeof(int), err)) != MBG_OK) return st;
+    if ((st = lalloc(L, (void**)&D->ghost_fast, gfast.size() * sizeof(GhostCell), err)) != MBG_OK) return st;
+    if ((st = lalloc(L, (void**)&D->ghost_rest, grest.size() * sizeof(GhostCell), err)) != MBG_OK) return st;
+    cudaMemcpy(D->gslots, gsl.data(), gsl.size() * sizeof(NbrSlot), cudaMemcpyHostToDevice);
+    cudaMemcpy(D->gslot_off, gsl_off.data(), gsl_off.size() * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(D->ghost_fast, gfast.data(), gfast.size() * sizeof(GhostCell), cudaMemcpyHostToDevice);
+    cudaMemcpy(D->ghost_rest, grest.data(), grest.size() * sizeof(GhostCell), cudaMemcpyHostToDevice);
     D->nsgather = (long long)sdst.size();
     D->nsgen = (long long)scell.size();
     if ((st = lalloc(L, (void**)&D->sdst, sdst.size() * sizeof(long long), err)) != MBG_OK) return st;
@@ -795,9 +919,10 @@ int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const Le
     }
     if (L.NG > 0 && plan.nghost_cells > 0) {
         run(LOWP_STAGE_GHOST_STREAM, [&] {
-            LOWP16(bf, ghost_gather, k, D->sdst, D->ssrc, D->nsgather, plan.ghost_list, D->scell, D->sq, D->nsgen, s);
+            LOWP16(bf, ghost_slots, k, D->gslots, D->gslot_off, D->gslot_lg, D->ghost_fast, D->nghost_fast, s);
+            LOWP16(bf, ghost_gather, k, D->sdst, D->ssrc, D->nsgather, D->ghost_rest, D->scell, D->sq, D->nsgen, s);
         });
-        ++launches;
+        launches += (D->nghost_fast > 0) + (D->nsgather > 0) + (D->nsgen > 0);
     }
     if (D->variant == 0 || D->variant == 3) {
         const bool pairs = D->variant == 0;

@@ -1141,6 +1141,46 @@ template <bool BF>
 __device__ __noinline__ float pull16_rt(int q, const LowpK* __restrict__ K, int b, int x, int y, int z,
                                         uint8_t tflag, int which);
 
+// ghost stream through the ghost-shell slot tables (mbg_lowp.cu::
+// ghost_slots16): the code of each pulled value, or the sentinel for a
+// source beyond the shell (Source/LBM.cpp:558-604 over the grown box)
+template <bool BF>
+__global__ void k_ghost_stream16s(const LowpK* __restrict__ K, const NbrSlot* __restrict__ T0,
+                                  const int* __restrict__ toff, int lg0, int lg1, int lg2,
+                                  const GhostCell* __restrict__ gl, long long n)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    const GhostCell gc = gl[e];
+    const LV16& L = K->L;
+    const DevBox& B = L.box[gc.box];
+    const NbrSlot* __restrict__ T = T0 + toff[gc.box];
+    const int top0 = ((B.n[0] + (1 << lg0) - 1) >> lg0) + 1, top1 = ((B.n[1] + (1 << lg1) - 1) >> lg1) + 1,
+              top2 = ((B.n[2] + (1 << lg2) - 1) >> lg2) + 1;
+    const int tx = top0 + 1, ty = top1 + 1;
+    const long long gi = B.goff + fab_lin(B, gc.x, gc.y, gc.z);
+    const u16* __restrict__ f = K->s.f;
+    const u16* __restrict__ g = K->s.g;
+    const u16* __restrict__ fg = K->s.fg;
+    const u16* __restrict__ gg = K->s.gg;
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        const int sx = gc.x - ev_x(q), sy = gc.y - ev_y(q), sz = gc.z - ev_z(q);
+        u16 cf = SENT16, cg = SENT16;
+        if (sx >= -3 && sy >= -3 && sz >= -3 && sx <= B.n[0] + 2 && sy <= B.n[1] + 2 && sz <= B.n[2] + 2) {
+            const int ox = sx < 0 ? 0 : (sx < B.n[0] ? (sx >> lg0) + 1 : top0);
+            const int oy = sy < 0 ? 0 : (sy < B.n[1] ? (sy >> lg1) + 1 : top1);
+            const int oz = sz < 0 ? 0 : (sz < B.n[2] ? (sz >> lg2) + 1 : top2);
+            const NbrSlot S = T[ox + tx * (oy + ty * oz)];
+            const long long i = S.base + (long long)sz * S.sz + (long long)sy * S.sy + sx;
+            cf = S.ghost ? fg[q * L.NG + i] : f[q * L.N + i];
+            cg = S.ghost ? gg[q * L.NG + i] : g[q * L.N + i];
+        }
+        K->fBg[q * L.NG + gi] = cf;
+        K->gBg[q * L.NG + gi] = cg;
+    }
+}
+
 // the ghost stream's remaining entries (bounce-back, physical BCs)
 template <bool BF>
 __global__ void k_ghost_general16(const LowpK* __restrict__ K, const GhostCell* __restrict__ gl,
@@ -1649,6 +1689,13 @@ template <bool BF>
 void Lowp16<BF>::ghost_stream(const LowpK* k, const GhostCell* gl, long long n, cudaStream_t s)
 {
     if (n > 0) k_ghost_stream16<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, gl, n);
+}
+template <bool BF>
+void Lowp16<BF>::ghost_slots(const LowpK* k, const NbrSlot* T, const int* off, const int lg[3], const GhostCell* gl,
+                             long long n, cudaStream_t s)
+{
+    if (n > 0)
+        k_ghost_stream16s<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, T, off, lg[0], lg[1], lg[2], gl, n);
 }
 template <bool BF>
 void Lowp16<BF>::ghost_gather(const LowpK* k, const long long* dst, const long long* src, long long n,
