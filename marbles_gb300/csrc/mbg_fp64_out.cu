@@ -239,8 +239,8 @@ __global__ void __launch_bounds__(TILE_CELLS) k_conserved(LV L, Phys64 ph, const
 // host layout [box][q][cell] <-> the FP64 state [q][N]: the staging pass of
 // mbg_set_state / mbg_get_state (one contiguous copy over the link instead
 // of one strided copy per box and lattice)
-__global__ void __launch_bounds__(TILE_CELLS) k_stage(LV L, const Tile* tiles, double* stage, double* v,
-                                                      int to_state)
+__global__ void __launch_bounds__(TILE_CELLS) k_stage(LV L, const Tile* __restrict__ tiles,
+                                                      double* __restrict__ stage, double* __restrict__ v, int to_state)
 {
     int b, x, y, z;
     long long c;

@@ -629,8 +629,8 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     std::vector<NbrSlot> gsl;
     std::vector<int> gsl_off;
     std::vector<GhostCell> gfast, grest;
+    std::vector<char> gok(box.size(), 0);
     if (host.ghosts && NG > 0) {
-        std::vector<char> gok;
         ghost_slots16(box, host, plan.slot_lg, gsl, gsl_off, gok);
         for (const GhostCell& gc : *host.ghosts) (gok[gc.box] ? gfast : grest).push_back(gc);
         ghost_plan(box, grest, L.N, NG, host, sdst, ssrc, scell, sq);
@@ -640,6 +640,10 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
     std::vector<long long> qdst, qsrc;
     std::vector<HaloCell> qghost;
     qpad_plan(box, halo, L.N, host, qdst, qsrc, qghost);
+    // the ghost stream of boxes with a ghost-shell table writes the Q_corr
+    // of their coarse-fine pad face cells itself
+    qghost.erase(std::remove_if(qghost.begin(), qghost.end(), [&](const HaloCell& c) { return gok[c.box] != 0; }),
+                 qghost.end());
     mbg_status st;
     if ((st = lalloc(L, (void**)&D->box16, box.size() * sizeof(DevBox), err)) != MBG_OK) return st;
     for (int v = 0; v < 2; ++v) {
@@ -919,7 +923,7 @@ int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const Le
     }
     if (L.NG > 0 && plan.nghost_cells > 0) {
         run(LOWP_STAGE_GHOST_STREAM, [&] {
-            LOWP16(bf, ghost_slots, k, D->gslots, D->gslot_off, D->gslot_lg, D->ghost_fast, D->nghost_fast, s);
+            LOWP16(bf, ghost_slots, k, D->gslots, D->gslot_off, D->gslot_lg, D->ghost_fast, D->nghost_fast, D->qs, s);
             LOWP16(bf, ghost_gather, k, D->sdst, D->ssrc, D->nsgather, D->ghost_rest, D->scell, D->sq, D->nsgen, s);
         });
         launches += (D->nghost_fast > 0) + (D->nsgather > 0) + (D->nsgen > 0);

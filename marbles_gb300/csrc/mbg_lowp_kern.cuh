@@ -188,11 +188,22 @@ __global__ void k_halo_copy16(const LowpK* __restrict__ K, const HaloCopy* __res
     const u16* __restrict__ f = own ? K->s.f + h.src : K->s.fg + (-h.src - 1);
     const u16* __restrict__ g = own ? K->s.g + h.src : K->s.gg + (-h.src - 1);
     const long long stride = own ? N : NG;
+    // every load before the first store: the pad is written in place in
+    // the source buffer, so the compiler would otherwise keep each load
+    // behind the previous direction's store (pad cells are never sources)
+    u16 vf[NQ], vg[NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
         if ((h.qmask >> q) & 1u) {
-            K->fA[q * N + h.dst] = f[q * stride];
-            K->gA[q * N + h.dst] = g[q * stride];
+            vf[q] = f[q * stride];
+            vg[q] = g[q * stride];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+        if ((h.qmask >> q) & 1u) {
+            K->fA[q * N + h.dst] = vf[q];
+            K->gA[q * N + h.dst] = vg[q];
         }
     }
 }
@@ -823,21 +834,22 @@ __device__ __forceinline__ PairOvr pair_ovr(const LowpK* __restrict__ K, const D
 // source, ov: its override buffer); an overwritten cell takes the override
 // code where it is not NOOVR16.  Pairs with an overwritten cell store the
 // merged pair back into the override buffer (idempotent: a merged code is
-// never NOOVR16), so that pass 2 reads one word there instead of merging.
+// never NOOVR16), so that pass 2 reads one word there instead of merging;
+// where both codes come from the override buffer (cells under the finer
+// level) nothing is pulled and nothing stored.
 template <int q>
 __device__ __forceinline__ unsigned code_merge(const u16* __restrict__ v, u16* __restrict__ ov, long long N,
                                                const PairOvr& o, int c, int sy, int sz)
 {
-    unsigned r = ld_pair<q>(v, c, sy, sz);
-    if (o.any) {
-        unsigned* w = reinterpret_cast<unsigned*>(ov + q * N + c);
-        const unsigned ow = *w;
-        unsigned m = 0u;
-        if (o.o0 && (ow & 0xFFFFu) != NOOVR16) m |= 0x0000FFFFu;
-        if (o.o1 && (ow >> 16) != NOOVR16) m |= 0xFFFF0000u;
-        r = (ow & m) | (r & ~m);
-        *w = r;
-    }
+    if (!o.any) return ld_pair<q>(v, c, sy, sz);
+    unsigned* w = reinterpret_cast<unsigned*>(ov + q * N + c);
+    const unsigned ow = *w;
+    unsigned m = 0u;
+    if (o.o0 && (ow & 0xFFFFu) != NOOVR16) m |= 0x0000FFFFu;
+    if (o.o1 && (ow >> 16) != NOOVR16) m |= 0xFFFF0000u;
+    if (m == 0xFFFFFFFFu) return ow;
+    const unsigned r = (ow & m) | (ld_pair<q>(v, c, sy, sz) & ~m);
+    *w = r;
     return r;
 }
 
@@ -1147,7 +1159,7 @@ __device__ __noinline__ float pull16_rt(int q, const LowpK* __restrict__ K, int 
 template <bool BF>
 __global__ void k_ghost_stream16s(const LowpK* __restrict__ K, const NbrSlot* __restrict__ T0,
                                   const int* __restrict__ toff, int lg0, int lg1, int lg2,
-                                  const GhostCell* __restrict__ gl, long long n)
+                                  const GhostCell* __restrict__ gl, long long n, float* __restrict__ qs)
 {
     const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
@@ -1163,21 +1175,45 @@ __global__ void k_ghost_stream16s(const LowpK* __restrict__ K, const NbrSlot* __
     const u16* __restrict__ g = K->s.g;
     const u16* __restrict__ fg = K->s.fg;
     const u16* __restrict__ gg = K->s.gg;
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
+    // a pad face cell (one coordinate one cell out) inside the domain box:
+    // its Q_corr normal to the face is the step's gradient input (the
+    // moments of the values streamed here, as k_qhalo16 takes them)
+    const int o0 = gc.x < 0 || gc.x >= B.n[0], o1 = gc.y < 0 || gc.y >= B.n[1], o2 = gc.z < 0 || gc.z >= B.n[2];
+    const bool face1 = o0 + o1 + o2 == 1 && gc.x >= -1 && gc.y >= -1 && gc.z >= -1 && gc.x <= B.n[0] &&
+                       gc.y <= B.n[1] && gc.z <= B.n[2] && B.lo[0] + gc.x >= L.dlo[0] &&
+                       B.lo[1] + gc.y >= L.dlo[1] && B.lo[2] + gc.z >= L.dlo[2] && B.lo[0] + gc.x <= L.dhi[0] &&
+                       B.lo[1] + gc.y <= L.dhi[1] && B.lo[2] + gc.z <= L.dhi[2];
+    // every code first, then the stores (the compiler cannot tell the
+    // destination ghost fab from the sources, so it would keep each load
+    // behind the previous direction's store)
+    u16 cf[NQ], cg[NQ];
+    static_for<0, NQ>([&](auto Q) {
+        constexpr int q = Q.value;
         const int sx = gc.x - ev_x(q), sy = gc.y - ev_y(q), sz = gc.z - ev_z(q);
-        u16 cf = SENT16, cg = SENT16;
+        cf[q] = SENT16;
+        cg[q] = SENT16;
         if (sx >= -3 && sy >= -3 && sz >= -3 && sx <= B.n[0] + 2 && sy <= B.n[1] + 2 && sz <= B.n[2] + 2) {
             const int ox = sx < 0 ? 0 : (sx < B.n[0] ? (sx >> lg0) + 1 : top0);
             const int oy = sy < 0 ? 0 : (sy < B.n[1] ? (sy >> lg1) + 1 : top1);
             const int oz = sz < 0 ? 0 : (sz < B.n[2] ? (sz >> lg2) + 1 : top2);
             const NbrSlot S = T[ox + tx * (oy + ty * oz)];
             const long long i = S.base + (long long)sz * S.sz + (long long)sy * S.sy + sx;
-            cf = S.ghost ? fg[q * L.NG + i] : f[q * L.N + i];
-            cg = S.ghost ? gg[q * L.NG + i] : g[q * L.N + i];
+            cf[q] = S.ghost ? fg[q * L.NG + i] : f[q * L.N + i];
+            cg[q] = S.ghost ? gg[q * L.NG + i] : g[q * L.N + i];
         }
-        K->fBg[q * L.NG + gi] = cf;
-        K->gBg[q * L.NG + gi] = cg;
+    });
+    MomentAcc<float> acc;
+    static_for<0, NQ>([&](auto Q) {
+        constexpr int q = Q.value;
+        K->fBg[q * L.NG + gi] = cf[q];
+        K->gBg[q * L.NG + gi] = cg[q];
+        if (face1) acc.template add<q>(dec<BF>(K->ct, cf[q], q, false), dec<BF>(K->ct, cg[q], q, true));
+    });
+    if (face1) {
+        const Macro<float> m = acc.finish(K->ph.mesh_speed, K->ph.Rg, K->ph.cv);
+        const int d = o0 ? 0 : o1 ? 1 : 2;
+        qs[d * L.N + B.voff + (long long)gc.z * B.sz + (long long)gc.y * B.sy + gc.x] =
+            d == 0 ? m.qcx : d == 1 ? m.qcy : m.qcz;
     }
 }
 
@@ -1692,10 +1728,10 @@ void Lowp16<BF>::ghost_stream(const LowpK* k, const GhostCell* gl, long long n, 
 }
 template <bool BF>
 void Lowp16<BF>::ghost_slots(const LowpK* k, const NbrSlot* T, const int* off, const int lg[3], const GhostCell* gl,
-                             long long n, cudaStream_t s)
+                             long long n, float* qs, cudaStream_t s)
 {
     if (n > 0)
-        k_ghost_stream16s<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, T, off, lg[0], lg[1], lg[2], gl, n);
+        k_ghost_stream16s<BF><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, T, off, lg[0], lg[1], lg[2], gl, n, qs);
 }
 template <bool BF>
 void Lowp16<BF>::ghost_gather(const LowpK* k, const long long* dst, const long long* src, long long n,

@@ -173,9 +173,11 @@ struct Lowp16 {
     static void ghost_gather(const LowpK* k, const long long* dst, const long long* src, long long n,
                              const GhostCell* gl, const int* gcell, const int* gq, long long ngen, cudaStream_t s);
     // the ghost stream of the ghost cells of all-fluid boxes with a
-    // ghost-shell slot table: a copy of the code each pull reads
+    // ghost-shell slot table: a copy of the code each pull reads; at the pad
+    // face cells inside the domain box also the Q_corr component normal to
+    // the face, into qs (the step's Q_corr array)
     static void ghost_slots(const LowpK* k, const NbrSlot* T, const int* off, const int lg[3], const GhostCell* gl,
-                            long long n, cudaStream_t s);
+                            long long n, float* qs, cudaStream_t s);
     // explosion: coarse neighbours, slopes and limiter per coarse cell, then
     // the fine ghost cells (3 launches)
     static void explode(const LowpK* kf, const LowpK* kc, const ExplodePlan& xp, u16* fg, u16* gg, cudaStream_t s);
