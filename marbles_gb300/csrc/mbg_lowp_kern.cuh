@@ -514,12 +514,14 @@ __global__ void __launch_bounds__(FT_THREADS, 2)
 }
 
 // ---- two-pass step ------------------------------------------------------------
-// pass 1 (k_qcorr16): Q_corr of every valid cell into qs[d * N + c], padded
-// layout; k_qhalo16 then fills the face cells of each box's pad with Q_corr
-// as the owning box (or, on the coarse-fine shell, the box itself) computes
-// it; pass 2 (k_collide16) pulls again, takes the gradient from qs and
-// collides.  No barriers and no halo recomputation; the populations are read
-// twice.
+// pass 1 (k_qcorr16, or k_qcorr16p on cell pairs): Q_corr of every valid cell
+// into qs[d * N + c], padded layout; the face cells of each box's pad then
+// get Q_corr as the owning box computes it (k_qpad_copy) or, on the
+// coarse-fine shell, as the box itself computes it from its ghost fab (the
+// ghost stream k_ghost_stream16s, or k_qhalo16 for boxes without a
+// ghost-shell table); pass 2 (k_collide16 / k_collide16p) pulls again, takes
+// the gradient from qs and collides.  No barriers and no halo recomputation;
+// the populations are read twice.
 
 // box-local cell of thread threadIdx.x of a Tile (128 cells in x-fastest order)
 __device__ __forceinline__ bool tile_cell(const DevBox& B, const Tile& t, int& x, int& y, int& z)
