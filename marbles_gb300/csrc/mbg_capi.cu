@@ -66,6 +66,10 @@ struct Level {
     int nfast = 0;
     Tile* d_fasteb_tiles = nullptr;
     int nfasteb = 0;
+    Tile* d_fastbc_tiles = nullptr;
+    int nfastbc = 0;
+    Tile* d_fastebbc_tiles = nullptr;
+    int nfastebbc = 0;
     Tile* d_gen_tiles = nullptr;
     int ngen = 0;
     GhostCell* d_ghost = nullptr;
@@ -262,8 +266,9 @@ static int owner_host(const Level& L, const int p[3])
 // domain side within one cell, no chunk across a box edge) and its table
 // fits; off[n] is the table's first slot, -1 for a box without one.
 static void build_slots(const Level& L, const int* is_periodic, const int lg[3], std::vector<NbrSlot>& out,
-                        std::vector<int>& off, std::vector<char>& ok, int w = 1)
+                        std::vector<int>& off, std::vector<char>& ok, int w = 1, std::vector<char>* has_bc = nullptr)
 {
+    if (has_bc) has_bc->assign(L.boxes.size(), 0);
     const int nbox = (int)L.boxes.size();
     out.clear();
     off.assign(nbox, -1);
@@ -312,11 +317,17 @@ static void build_slots(const Level& L, const int* is_periodic, const int lg[3],
                     int owner = -2;         // -2: unset, -1: uncovered
                     int delta[3] = {0, 0, 0};
                     bool good = true;
+                    long long outside = 0, cells = 0;
                     for (int z = rlo[2]; z <= rhi[2] && good; ++z)
                         for (int y = rlo[1]; y <= rhi[1] && good; ++y)
                             for (int x = rlo[0]; x <= rhi[0] && good; ++x) {
                                 int gp[3] = {b.lo[0] + x, b.lo[1] + y, b.lo[2] + z};
-                                if (!wrap_host(L, is_periodic, gp)) { good = false; break; }
+                                ++cells;
+                                if (!wrap_host(L, is_periodic, gp)) {
+                                    ++outside;   // beyond a non-periodic side
+                                    continue;
+                                }
+                                if (outside > 0) { good = false; break; }
                                 const int o = owner_host(L, gp);
                                 int dl[3] = {0, 0, 0};
                                 if (o >= 0) {
@@ -331,7 +342,16 @@ static void build_slots(const Level& L, const int* is_periodic, const int lg[3],
                                     good = false;
                                 }
                             }
-                    if (good && owner >= 0) {
+                    if (good && outside > 0) {
+                        // the step tables take a chunk wholly beyond a
+                        // non-periodic side: its pulls are the BC's values
+                        if (outside == cells && w == 1 && has_bc) {
+                            S.ghost = 2;
+                            (*has_bc)[n] = 1;
+                        } else {
+                            all = false;
+                        }
+                    } else if (good && owner >= 0) {
                         const DevBox& O = L.hbox[owner];
                         S.base = O.voff + (long long)delta[2] * O.sz + (long long)delta[1] * O.sy + delta[0];
                         S.sy = O.sy;
@@ -398,6 +418,10 @@ static void refresh_plan(mbg_ctx* ctx, Level& L)
     L.plan.nfast = L.nfast;
     L.plan.fasteb_tiles = L.d_fasteb_tiles;
     L.plan.nfasteb = L.nfasteb;
+    L.plan.fastbc_tiles = L.d_fastbc_tiles;
+    L.plan.nfastbc = L.nfastbc;
+    L.plan.fastebbc_tiles = L.d_fastebbc_tiles;
+    L.plan.nfastebbc = L.nfastebbc;
     L.plan.gen_tiles = L.d_gen_tiles;
     L.plan.ngen = L.ngen;
     L.plan.ghost_list = L.d_ghost;
@@ -758,12 +782,13 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     MBG_CUDA(cudaMemcpyAsync(L.d_omap, L.omap.data(), L.omap.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->s));
     if ((st = dalloc(ctx, &L.d_flags, L.hflags.size())) != MBG_OK) return st;
     MBG_CUDA(cudaMemcpyAsync(L.d_flags, L.hflags.data(), L.hflags.size(), cudaMemcpyHostToDevice, ctx->s));
-    std::vector<Tile> tiles, fast_tiles, fasteb_tiles, gen_tiles;
+    std::vector<Tile> tiles, fast_tiles, fasteb_tiles, fastbc_tiles, fastebbc_tiles, gen_tiles;
     std::vector<NbrSlot> slots;
     std::vector<int> slot_off;
     std::vector<char> slot_ok;
     for (int d = 0; d < 3; ++d) L.slot_lg[d] = slot_lg(L, d);
-    build_slots(L, p.is_periodic, L.slot_lg, slots, slot_off, slot_ok);
+    std::vector<char> slot_bc;
+    build_slots(L, p.is_periodic, L.slot_lg, slots, slot_off, slot_ok, 1, &slot_bc);
     L.slot_max = 0;
     for (int n = 0; n < nbox; ++n) {
         const bool simple = slot_ok[n];
@@ -772,7 +797,9 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
             for (int d = 0; d < 3; ++d) t *= ((L.boxes[n].n(d) + (1 << L.slot_lg[d]) - 1) >> L.slot_lg[d]) + 2;
             L.slot_max = std::max(L.slot_max, t);
         }
-        std::vector<Tile>& list = !simple ? gen_tiles : (L.hbox[n].all_fluid ? fast_tiles : fasteb_tiles);
+        std::vector<Tile>& list = !simple ? gen_tiles
+                                  : slot_bc[n] ? (L.hbox[n].all_fluid ? fastbc_tiles : fastebbc_tiles)
+                                               : (L.hbox[n].all_fluid ? fast_tiles : fasteb_tiles);
         for (long long s = 0; s < L.boxes[n].vol(); s += TILE_CELLS) {
             tiles.push_back(Tile{n, (int)s});
             list.push_back(Tile{n, (int)s});
@@ -781,12 +808,22 @@ mbg_status mbg_define_level(mbg_ctx* ctx, int lev, int nbox, const int* lohi, co
     L.ntiles = (int)tiles.size();
     L.nfast = (int)fast_tiles.size();
     L.nfasteb = (int)fasteb_tiles.size();
+    L.nfastbc = (int)fastbc_tiles.size();
+    L.nfastebbc = (int)fastebbc_tiles.size();
     L.ngen = (int)gen_tiles.size();
     if ((st = dalloc(ctx, &L.d_tiles, tiles.size())) != MBG_OK) return st;
     MBG_CUDA(cudaMemcpyAsync(L.d_tiles, tiles.data(), tiles.size() * sizeof(Tile), cudaMemcpyHostToDevice, ctx->s));
     if ((st = dalloc(ctx, &L.d_fast_tiles, fast_tiles.size())) != MBG_OK) return st;
     if ((st = dalloc(ctx, &L.d_gen_tiles, gen_tiles.size())) != MBG_OK) return st;
     if ((st = dalloc(ctx, &L.d_fasteb_tiles, fasteb_tiles.size())) != MBG_OK) return st;
+    if ((st = dalloc(ctx, &L.d_fastbc_tiles, fastbc_tiles.size())) != MBG_OK) return st;
+    if ((st = dalloc(ctx, &L.d_fastebbc_tiles, fastebbc_tiles.size())) != MBG_OK) return st;
+    if (!fastbc_tiles.empty())
+        MBG_CUDA(cudaMemcpyAsync(L.d_fastbc_tiles, fastbc_tiles.data(), fastbc_tiles.size() * sizeof(Tile),
+                                 cudaMemcpyHostToDevice, ctx->s));
+    if (!fastebbc_tiles.empty())
+        MBG_CUDA(cudaMemcpyAsync(L.d_fastebbc_tiles, fastebbc_tiles.data(), fastebbc_tiles.size() * sizeof(Tile),
+                                 cudaMemcpyHostToDevice, ctx->s));
     if (!fasteb_tiles.empty())
         MBG_CUDA(cudaMemcpyAsync(L.d_fasteb_tiles, fasteb_tiles.data(), fasteb_tiles.size() * sizeof(Tile),
                                  cudaMemcpyHostToDevice, ctx->s));

@@ -57,6 +57,25 @@ __device__ __forceinline__ double pull_slot(const SlotTab& T, const DevBox& B, i
     return s.ghost ? vg[q * NG + i] : v[q * N + i];
 }
 
+// boxes within one cell of a non-periodic side: a chunk beyond it (ghost =
+// 2) gives the general pull, whose BC functor computes the value
+// (Source/BC.H:345-471); every other chunk reads through the table
+template <int q>
+__device__ __forceinline__ double pull_slot_bc(const LV& L, const BCParams& P, const SlotTab& T, const DevBox& B,
+                                               int x, int y, int z, uint8_t tf, const double* v, const double* vg,
+                                               bool is_g, const Lattice<double>& lat)
+{
+    constexpr int ex = ev_x(q), ey = ev_y(q), ez = ev_z(q);
+    const int sx = x - ex, sy = y - ey, sz = z - ez;
+    const int ox = ex == 0 ? (x >> T.lg[0]) + 1 : chunk_of(sx, B.n[0], T.lg[0], T.top[0]);
+    const int oy = ey == 0 ? (y >> T.lg[1]) + 1 : chunk_of(sy, B.n[1], T.lg[1], T.top[1]);
+    const int oz = ez == 0 ? (z >> T.lg[2]) + 1 : chunk_of(sz, B.n[2], T.lg[2], T.top[2]);
+    const NbrSlot& s = T.s[ox + T.tx * (oy + T.ty * oz)];
+    if (s.ghost == 2) return pull<q>(L, P, B, x, y, z, tf, false, v, vg, is_g, lat);
+    const long long i = s.base + (long long)sz * s.sz + (long long)sy * s.sy + sx;
+    return s.ghost ? vg[q * L.NG + i] : v[q * L.N + i];
+}
+
 // the same in a box holding solid cells: a solid source bounces back the
 // target's own opposite population (the half-way bounce-back of the push,
 // Source/LBM.cpp:574-598)
@@ -68,6 +87,17 @@ __device__ __forceinline__ double pull_slot_eb(const LV& L, const SlotTab& T, co
     if (!(flag_at(L, B, x - ev_x(q), y - ev_y(q), z - ev_z(q)) & FL_FLUID))
         return v[oq * L.N + B.voff + val_lin(B, x, y, z)];
     return pull_slot<q>(T, B, x, y, z, v, vg, L.N, L.NG);
+}
+
+template <int q>
+__device__ __forceinline__ double pull_slot_eb_bc(const LV& L, const BCParams& P, const SlotTab& T, const DevBox& B,
+                                                  int x, int y, int z, uint8_t tf, const double* v, const double* vg,
+                                                  bool is_g, const Lattice<double>& lat)
+{
+    constexpr int oq = opp(q);
+    if (!(flag_at(L, B, x - ev_x(q), y - ev_y(q), z - ev_z(q)) & FL_FLUID))
+        return v[oq * L.N + B.voff + val_lin(B, x, y, z)];
+    return pull_slot_bc<q>(L, P, T, B, x, y, z, tf, v, vg, is_g, lat);
 }
 
 // Q_corr component d at box-local neighbour (x, y, z) through the slot table
@@ -146,7 +176,8 @@ __device__ __forceinline__ bool tile_setup(const LV& L, const LevelPlan& lp, con
 
 // ---- pass 1: stream + macro fields ----------------------------------------
 // MODE 0: general pull; 1: neighbour slots, all-fluid box; 2: neighbour
-// slots, box holding solid cells
+// slots, box holding solid cells; 3 and 4: the same for boxes within one cell
+// of a non-periodic side (chunks beyond it through the BC functor)
 template <int MODE>
 __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, LevelPlan lp, BCParams P, Phys64 ph, const Tile* tiles,
                                                         const double* fA, const double* gA, const double* fAg,
@@ -167,9 +198,13 @@ __global__ void __launch_bounds__(TILE_CELLS) k_moments(LV L, LevelPlan lp, BCPa
     MomentAcc<double> acc;
 #define MBG_PULLF(q) (MODE == 1 ? pull_slot<q>(T, B, x, y, z, fA, fAg, L.N, L.NG)                  \
                      : MODE == 2 ? pull_slot_eb<q>(L, T, B, x, y, z, fA, fAg)                       \
+                     : MODE == 3 ? pull_slot_bc<q>(L, P, T, B, x, y, z, tf, fA, fAg, false, ph.lat)  \
+                     : MODE == 4 ? pull_slot_eb_bc<q>(L, P, T, B, x, y, z, tf, fA, fAg, false, ph.lat) \
                                  : pull<q>(L, P, B, x, y, z, tf, interior, fA, fAg, false, ph.lat))
 #define MBG_PULLG(q) (MODE == 1 ? pull_slot<q>(T, B, x, y, z, gA, gAg, L.N, L.NG)                  \
                      : MODE == 2 ? pull_slot_eb<q>(L, T, B, x, y, z, gA, gAg)                       \
+                     : MODE == 3 ? pull_slot_bc<q>(L, P, T, B, x, y, z, tf, gA, gAg, true, ph.lat)   \
+                     : MODE == 4 ? pull_slot_eb_bc<q>(L, P, T, B, x, y, z, tf, gA, gAg, true, ph.lat) \
                                  : pull<q>(L, P, B, x, y, z, tf, interior, gA, gAg, true, ph.lat))
 #define MBG_M64(q)                                                             \
     {                                                                          \
@@ -248,9 +283,9 @@ __global__ void __launch_bounds__(TILE_CELLS) k_collide(LV L, LevelPlan lp, BCPa
     m.temp = md[MD_T * N + cell];
     double dqx, dqy, dqz;
     if (MODE > 0) {
-        dqx = qgrad_slot<MODE == 2>(L, T, B, x, y, z, 0, ph.idx[0], md, gqc);
-        dqy = qgrad_slot<MODE == 2>(L, T, B, x, y, z, 1, ph.idx[1], md, gqc);
-        dqz = qgrad_slot<MODE == 2>(L, T, B, x, y, z, 2, ph.idx[2], md, gqc);
+        dqx = qgrad_slot<MODE == 2 || MODE == 4>(L, T, B, x, y, z, 0, ph.idx[0], md, gqc);
+        dqy = qgrad_slot<MODE == 2 || MODE == 4>(L, T, B, x, y, z, 1, ph.idx[1], md, gqc);
+        dqz = qgrad_slot<MODE == 2 || MODE == 4>(L, T, B, x, y, z, 2, ph.idx[2], md, gqc);
     } else {
         dqx = qgrad(L, B, x, y, z, 0, ph.idx[0], md, gqc);
         dqy = qgrad(L, B, x, y, z, 1, ph.idx[1], md, gqc);
@@ -296,6 +331,11 @@ void launch_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, co
         k_moments<1><<<lp.nfast, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fast_tiles, fA, gA, fAg, gAg, fB, gB, md);
     if (lp.nfasteb > 0)
         k_moments<2><<<lp.nfasteb, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fasteb_tiles, fA, gA, fAg, gAg, fB, gB, md);
+    if (lp.nfastbc > 0)
+        k_moments<3><<<lp.nfastbc, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fastbc_tiles, fA, gA, fAg, gAg, fB, gB, md);
+    if (lp.nfastebbc > 0)
+        k_moments<4><<<lp.nfastebbc, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fastebbc_tiles, fA, gA, fAg, gAg, fB, gB,
+                                                          md);
     if (lp.ngen > 0)
         k_moments<0><<<lp.ngen, TILE_CELLS, 0, s>>>(L, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB, gB, md);
 }
@@ -311,10 +351,19 @@ void launch_collide(const LevelPlan& lp, const BCParams& P, const Phys64& ph, co
     if (lp.nfasteb > 0)
         k_collide<2><<<lp.nfasteb, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fasteb_tiles, fA, gA, fAg, gAg, fB, gB, md,
                                                         gqc);
+    if (lp.nfastbc > 0)
+        k_collide<3><<<lp.nfastbc, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fastbc_tiles, fA, gA, fAg, gAg, fB, gB, md,
+                                                        gqc);
+    if (lp.nfastebbc > 0)
+        k_collide<4><<<lp.nfastebbc, TILE_CELLS, sb, s>>>(L, lp, P, ph, lp.fastebbc_tiles, fA, gA, fAg, gAg, fB, gB,
+                                                          md, gqc);
     if (lp.ngen > 0)
         k_collide<0><<<lp.ngen, TILE_CELLS, 0, s>>>(L, lp, P, ph, lp.gen_tiles, fA, gA, fAg, gAg, fB, gB, md, gqc);
 }
 
-int fp64_step_launches(const LevelPlan& lp) { return (lp.nfast > 0) + (lp.nfasteb > 0) + (lp.ngen > 0); }
+int fp64_step_launches(const LevelPlan& lp)
+{
+    return (lp.nfast > 0) + (lp.nfasteb > 0) + (lp.nfastbc > 0) + (lp.nfastebbc > 0) + (lp.ngen > 0);
+}
 
 }  // namespace mbg

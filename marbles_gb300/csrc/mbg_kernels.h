@@ -73,7 +73,7 @@ struct Phys32 {
 struct NbrSlot {
     long long base;
     int sy, sz;
-    int ghost;
+    int ghost;   // 0: valid cells, 1: the box's ghost fab, 2: beyond a non-periodic side (step tables)
     int pad;
 };
 constexpr int SLOT_TABLE_MAX = 1024;   // slots of one box's table (24 KB of shared memory)
@@ -94,6 +94,12 @@ struct LevelPlan {
     int nfast = 0;
     const Tile* fasteb_tiles = nullptr;   // the same for boxes holding solid cells
     int nfasteb = 0;
+    // the same two for boxes within one cell of a non-periodic side, whose
+    // tables mark the chunks beyond it (ghost = 2: the BC's values)
+    const Tile* fastbc_tiles = nullptr;
+    int nfastbc = 0;
+    const Tile* fastebbc_tiles = nullptr;
+    int nfastebbc = 0;
     const Tile* gen_tiles = nullptr;
     int ngen = 0;
     const GhostCell* ghost_list = nullptr;   // all uncovered ghost cells
