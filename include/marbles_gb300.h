@@ -175,6 +175,17 @@ mbg_status mbg_get_derived(mbg_ctx* ctx, int lev, double* derived);
  * the EB-force sum, Source/LBM.cpp:1040); one reduction launch per level. */
 mbg_status mbg_conserved(mbg_ctx* ctx, double out[5]);
 
+/* State check (the debug scans of the plan's auxiliary subsystems; no
+ * counterpart in the reference): every valid cell of every level is
+ * scanned on the device.  A fluid cell must hold finite populations other
+ * than the stream's -1 sentinel; a solid cell not overwritten by
+ * coalescence the sentinel in every direction.  counts = {bad values at
+ * fluid cells, bad values at solid cells}; first = {level, box, cell in the
+ * box (x fastest), 2 q + lattice} of the first bad value in that order, or
+ * -1 four times when there is none.  The 16-bit forms scan their decoded
+ * state.  The state is not changed. */
+mbg_status mbg_check_state(mbg_ctx* ctx, long long counts[2], long long first[4]);
+
 /* Wait for all work queued on the context's stream; reports a latched
  * device-side error. */
 mbg_status mbg_synchronize(mbg_ctx* ctx);

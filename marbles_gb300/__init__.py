@@ -28,7 +28,7 @@ EXPORTS = [
     "mbg_lbm_level_boxes", "mbg_lbm_level_flags", "mbg_lbm_write_plotfile", "mbg_lbm_last_error",
     "mbg_lbm_destroy", "mbg_lbm_write_checkpoint", "mbg_lbm_step_time", "mbg_tag_cells", "mbg_regrid", "mbg_lbm_regrid",
     "mbg_geometry_flags",
-    "mbg_get_derived", "mbg_conserved", "mbg_autotune", "mbg_tuning", "mbg_set_variant",
+    "mbg_get_derived", "mbg_conserved", "mbg_check_state", "mbg_autotune", "mbg_tuning", "mbg_set_variant",
     "mbg_write_plotfile", "mbg_write_multifab", "mbg_read_multifab",
     "mbg_batch_create", "mbg_batch_cells", "mbg_batch_set_state", "mbg_batch_get_state", "mbg_batch_get_macro",
     "mbg_batch_step", "mbg_batch_autotune", "mbg_batch_tuning", "mbg_batch_synchronize", "mbg_batch_launch_count",
@@ -336,6 +336,15 @@ class Context:
         out = np.zeros(5)
         self._check(self.L.mbg_conserved(self.h, _dp(out)), "mbg_conserved")
         return out
+
+    def check_state(self):
+        """((bad values at fluid cells, at solid cells), (level, box, cell,
+        2 q + lattice) of the first, or -1s): the state scan of
+        mbg_check_state."""
+        counts = (C.c_longlong * 2)()
+        first = (C.c_longlong * 4)()
+        self._check(self.L.mbg_check_state(self.h, counts, first), "mbg_check_state")
+        return (counts[0], counts[1]), tuple(first)
 
     def eb_forces(self):
         out = np.zeros(3)

@@ -125,6 +125,7 @@ struct mbg_ctx {
     std::string err;
     long long launches = 0;
     double* d_red = nullptr;   // small reduction scratch
+    unsigned long long* d_check = nullptr;   // mbg_check_state: two counts and the first key
     double* d_out19 = nullptr;
     size_t out19_n = 0;
     double* d_stage = nullptr;   // FP64 state transfers: one lattice of a level in host layout
@@ -1346,6 +1347,41 @@ mbg_status mbg_eb_forces(mbg_ctx* ctx, double out[3])
     MBG_CUDA(cudaGetLastError());
     MBG_CUDA(cudaMemcpyAsync(out, ctx->d_red, 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->s));
     MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    return MBG_OK;
+}
+
+mbg_status mbg_check_state(mbg_ctx* ctx, long long counts[2], long long first[4])
+{
+    if (!ctx || !counts || !first) return MBG_EINVAL;
+    if (ctx->lv.empty()) return fail(ctx, MBG_ESTATE, "mbg_check_state: no level defined");
+    if (!ctx->d_check) {
+        mbg_status st = dalloc(ctx, &ctx->d_check, 3);
+        if (st != MBG_OK) return st;
+    }
+    const unsigned long long init[3] = {0ULL, 0ULL, ~0ULL};
+    MBG_CUDA(cudaMemcpyAsync(ctx->d_check, init, sizeof(init), cudaMemcpyHostToDevice, ctx->s));
+    for (int lev = 0; lev < (int)ctx->lv.size(); ++lev) {
+        Level& L = ctx->lv[lev];
+        const double *f, *g, *fg, *gg;
+        mbg_status st = fp64_state(ctx, L, true, &f, &g, &fg, &gg);
+        if (st != MBG_OK) return st;
+        launch_check(L.plan, f, g, lev, ctx->d_check, ctx->s);
+        ctx->launches++;
+    }
+    MBG_CUDA(cudaGetLastError());
+    unsigned long long out[3];
+    MBG_CUDA(cudaMemcpyAsync(out, ctx->d_check, sizeof(out), cudaMemcpyDeviceToHost, ctx->s));
+    MBG_CUDA(cudaStreamSynchronize(ctx->s));
+    counts[0] = (long long)out[0];
+    counts[1] = (long long)out[1];
+    if (out[2] == ~0ULL) {
+        for (int i = 0; i < 4; ++i) first[i] = -1;
+    } else {
+        first[0] = (long long)(out[2] >> 58);
+        first[1] = (long long)((out[2] >> 38) & 0xFFFFFULL);
+        first[2] = (long long)((out[2] >> 7) & 0x7FFFFFFFULL);
+        first[3] = (long long)(out[2] & 0x7FULL);
+    }
     return MBG_OK;
 }
 

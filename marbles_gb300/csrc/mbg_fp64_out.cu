@@ -236,6 +236,48 @@ __global__ void __launch_bounds__(TILE_CELLS) k_conserved(LV L, Phys64 ph, const
         for (int k = 0; k < 5; ++k) atomicAdd(&out5[k], red[k][0]);
 }
 
+// NaN and sentinel scan of one level's FP64 (or decoded) state: counts of
+// bad values at fluid and at solid cells into out[0..1], the first bad value
+// (level, box, cell, 2 q + lattice as one ordered key) by an integer
+// minimum into out[2] -- both order-free, so the result is the same bits on
+// every call
+__global__ void __launch_bounds__(TILE_CELLS) k_check(LV L, const Tile* __restrict__ tiles,
+                                                      const double* __restrict__ f, const double* __restrict__ g,
+                                                      int lev, unsigned long long* __restrict__ out)
+{
+    int b, x, y, z;
+    long long c;
+    if (!cell_of_tile(L, tiles, b, x, y, z, c)) return;
+    const DevBox& B = L.box[b];
+    const uint8_t tf = flag_at(L, B, x, y, z);
+    const long long cell = B.voff + c;
+    const bool fluid = tf & FL_FLUID;
+    const bool ovr = tf & FL_OVR;
+    unsigned bad = 0u;
+    int first = -1;
+    for (int q = 0; q < NQ; ++q)
+        for (int lat = 0; lat < 2; ++lat) {
+            const double v = (lat ? g : f)[q * L.N + cell];
+            const bool wrong = fluid ? (!isfinite(v) || v == -1.0) : (!ovr && v != -1.0);
+            if (wrong) {
+                ++bad;
+                if (first < 0) first = 2 * q + lat;
+            }
+        }
+    if (bad) {
+        atomicAdd(&out[fluid ? 0 : 1], (unsigned long long)bad);
+        const unsigned long long key = ((unsigned long long)lev << 58) | ((unsigned long long)b << 38) |
+                                       ((unsigned long long)c << 7) | (unsigned long long)first;
+        atomicMin(&out[2], key);
+    }
+}
+
+void launch_check(const LevelPlan& lp, const double* f, const double* g, int lev, unsigned long long* out,
+                  cudaStream_t s)
+{
+    if (lp.ntiles > 0) k_check<<<lp.ntiles, TILE_CELLS, 0, s>>>(lp.view64, lp.tiles, f, g, lev, out);
+}
+
 // host layout [box][q][cell] <-> the FP64 state [q][N]: the staging pass of
 // mbg_set_state / mbg_get_state (one contiguous copy over the link instead
 // of one strided copy per box and lattice)

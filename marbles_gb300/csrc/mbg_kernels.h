@@ -166,6 +166,10 @@ void launch_coalesce(const LevelPlan& crse, const LevelPlan& fine, const BCParam
                      const CoalesceCell* list, long long n, const double* ff, const double* gf, const double* ffg,
                      const double* gfg, const double* fcA, const double* gcA, const double* fcAg,
                      const double* gcAg, double* fcB, double* gcB, int into_state, cudaStream_t s);
+// NaN and sentinel scan of a level's FP64 (or decoded) state into out[0..2]
+// (counts at fluid and at solid cells, key of the first bad value)
+void launch_check(const LevelPlan& lp, const double* f, const double* g, int lev, unsigned long long* out,
+                  cudaStream_t s);
 // host layout [box][q][cell] (stage) <-> FP64 state v [q][N], to_state: into v
 void launch_stage(const LevelPlan& lp, double* stage, double* v, int to_state, cudaStream_t s);
 void launch_macro_local(const LevelPlan& lp, const Phys64& ph, const double* f, const double* g, double* out19,

@@ -201,3 +201,31 @@ def test_evolve_writes_plotfiles_and_checkpoints_at_their_intervals(tmp_path):
     # plotfiles at 0, 2, 4 and the last step 5; checkpoints at 0 and 3
     assert names == ["chk00000", "chk00003", "plt00000", "plt00002", "plt00004", "plt00005"], names
     assert open(tmp_path / "chk00003" / "Header").readline().strip() == "Checkpoint file for LBM"
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_state_check_counts_a_planted_nan(prec):
+    """mbg_check_state: the state after a few steps of an inflow/outflow
+    sphere scans clean (fluid values finite, solid cells at the sentinel);
+    a NaN planted at one direction of one fluid cell is counted once and
+    located (level 0, box 0, cell 0, direction 5 of f)."""
+    import marbles_gb300 as M
+    p, levels = cases.sphere_channel(32, 16, 16, radius=4.0, center=(12.0, 8.0, 8.0), mgs=16, t0=0.03)
+    o = cases.run_oracle(p, levels, 0)
+    flags = o.get_grown_flags(0)
+    b0 = levels[0][0]
+    n = b0[3:] - b0[:3] + 1
+    assert flags[(3 * (n[1] + 6) + 3) * (n[0] + 6) + 3] & 1        # cell 0 of box 0 is fluid
+    c = M.Context(cases.mbg_params_from(p, prec))
+    c.define_level(0, levels[0], flags)
+    c.set_state(0, *o.get_state(0))
+    c.step(3)
+    counts, first = c.check_state()
+    assert counts == (0, 0) and first == (-1, -1, -1, -1)
+    f, g = c.get_state(0)
+    vol = int(np.prod(n))
+    f = f.copy()
+    f[5 * vol + 0] = np.nan
+    c.set_state(0, f, g)
+    counts, first = c.check_state()
+    assert counts == (1, 0) and first == (0, 0, 0, 10), (counts, first)
