@@ -44,7 +44,6 @@ struct LowpDev {
     int nctiles = 0;
     unsigned* nmask = nullptr;   // neighbour masks (neighbour_masks), or null
     std::vector<DevBox> box16h;  // host copy of box16
-    HaloCell* halo = nullptr;    // every pad cell of every box
     HaloCopy* hcopy = nullptr;   // pad fill: per pad cell, the directions and the cell copied (halo_plan)
     long long ngather = 0;
     HaloCell* general = nullptr; // pad cells that need the general kernel (physical BCs)
@@ -62,7 +61,7 @@ struct LowpDev {
     int* scell = nullptr;        // ghost stream entries for the general kernel
     int* sq = nullptr;
     long long nsgen = 0;
-    long long nhalo = 0;
+    long long nhalo = 0;         // pad cells of the level (the pad fill runs when there are any)
     u16* fo = nullptr;           // coalescence override buffers
     u16* go = nullptr;
     ExplodePlan xp{};            // explosion into this (fine) level's ghost fabs
@@ -687,7 +686,6 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
         D->qpad.ghost = qg;
         D->qpad.nghost = (long long)qghost.size();
     }
-    if ((st = lalloc(L, (void**)&D->halo, halo.size() * sizeof(HaloCell), err)) != MBG_OK) return st;
     D->ngather = (long long)hcopy.size();
     D->ngeneral = (long long)general.size();
     if ((st = lalloc(L, (void**)&D->hcopy, hcopy.size() * sizeof(HaloCopy), err)) != MBG_OK) return st;
@@ -731,7 +729,6 @@ mbg_status lowp_define(const mbg_params& p, const LevelPlan& plan, const std::ve
         cudaMemcpy((void*)xp.xc, xc.data(), xc.size() * sizeof(XSlot), cudaMemcpyHostToDevice);
     }
     cudaMemcpy(D->box16, box.data(), box.size() * sizeof(DevBox), cudaMemcpyHostToDevice);
-    cudaMemcpy(D->halo, halo.data(), halo.size() * sizeof(HaloCell), cudaMemcpyHostToDevice);
     const size_t sb = (size_t)L.N * NQ * 2;
     for (int b = 0; b < 2; ++b) {
         if ((st = lalloc(L, &L.f[b], sb, err)) != MBG_OK) return st;
@@ -919,7 +916,7 @@ int lowp_advance(const mbg_params& p, const BCParams& bc, LowpLevel& L, const Le
             LOWP16(bf, halo_copy, k, D->hcopy, D->ngather, s);
             LOWP16(bf, halo, k, D->general, D->ngeneral, s);
         });
-        ++launches;
+        launches += (D->ngather > 0) + (D->ngeneral > 0);
     }
     if (L.NG > 0 && plan.nghost_cells > 0) {
         run(LOWP_STAGE_GHOST_STREAM, [&] {
