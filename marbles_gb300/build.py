@@ -19,6 +19,8 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
           "--expt-relaxed-constexpr"] + ARCH
 UNITS = {
     "mbg_fp64.cu": ["-fmad=false"],
+    "mbg_fp64_bc.cu": ["-fmad=false"],
+    "mbg_fp64_gen.cu": ["-fmad=false"],
     "mbg_fp64_shell.cu": ["-fmad=false"],
     "mbg_fp64_amr.cu": ["-fmad=false"],
     "mbg_fp64_out.cu": ["-fmad=false"],

@@ -133,6 +133,20 @@ void launch_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, co
 void launch_collide(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
                     const double* fAg, const double* gAg, double* fB, double* gB, const double* md,
                     const double* gqc, cudaStream_t s);
+// the step kernels of modes 3-4 (mbg_fp64_bc.cu) and 0 (mbg_fp64_gen.cu),
+// called by launch_moments / launch_collide
+void launch_moments_bc(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
+                       const double* fAg, const double* gAg, const double* fB, const double* gB, double* md,
+                       cudaStream_t s);
+void launch_collide_bc(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
+                       const double* fAg, const double* gAg, double* fB, double* gB, const double* md,
+                       const double* gqc, cudaStream_t s);
+void launch_moments_gen(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
+                        const double* fAg, const double* gAg, const double* fB, const double* gB, double* md,
+                        cudaStream_t s);
+void launch_collide_gen(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
+                        const double* fAg, const double* gAg, double* fB, double* gB, const double* md,
+                        const double* gqc, cudaStream_t s);
 // the refinement criteria of one mbg_tag_cells call
 struct TagSet {
     int n = 0;
