@@ -20,6 +20,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
 UNITS = {
     "mbg_fp64.cu": ["-fmad=false"],
     "mbg_fp64_bc.cu": ["-fmad=false"],
+    "mbg_fp64_bcc.cu": ["-fmad=false"],
     "mbg_fp64_gen.cu": ["-fmad=false"],
     "mbg_fp64_shell.cu": ["-fmad=false"],
     "mbg_fp64_amr.cu": ["-fmad=false"],

@@ -1,8 +1,8 @@
 // mbg_fp64_step.cuh -- the FP64 level step's kernels (k_moments, k_collide)
 // and their neighbour-slot pulls, shared by the units that instantiate them:
-// mbg_fp64.cu (modes 1 and 2), mbg_fp64_bc.cu (modes 3 and 4) and
-// mbg_fp64_gen.cu (mode 0), so that the parallel build compiles the modes
-// side by side.  Every including unit is compiled with -fmad=false.
+// mbg_fp64.cu (modes 1 and 2), mbg_fp64_bc.cu and mbg_fp64_bcc.cu (modes 3
+// and 4, moment and collision pass) and mbg_fp64_gen.cu (mode 0), so that
+// the parallel build compiles them side by side.  Every including unit is compiled with -fmad=false.
 //
 // A level advance is two passes over the valid cells, each launched over up
 // to five tile lists: boxes whose neighbourhood the chunked slot tables

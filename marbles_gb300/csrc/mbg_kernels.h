@@ -133,8 +133,8 @@ void launch_moments(const LevelPlan& lp, const BCParams& P, const Phys64& ph, co
 void launch_collide(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
                     const double* fAg, const double* gAg, double* fB, double* gB, const double* md,
                     const double* gqc, cudaStream_t s);
-// the step kernels of modes 3-4 (mbg_fp64_bc.cu) and 0 (mbg_fp64_gen.cu),
-// called by launch_moments / launch_collide
+// the step kernels of modes 3-4 (mbg_fp64_bc.cu, mbg_fp64_bcc.cu) and 0
+// (mbg_fp64_gen.cu), called by launch_moments / launch_collide
 void launch_moments_bc(const LevelPlan& lp, const BCParams& P, const Phys64& ph, const double* fA, const double* gA,
                        const double* fAg, const double* gAg, const double* fB, const double* gB, double* md,
                        cudaStream_t s);
